@@ -1,0 +1,333 @@
+"""Benchmark of the PRK 2D stencil hot path on GB300.
+
+Workload (one "step" = one fused application over the whole grid: out += S(in) on the interior and
+in_next = in + 1 everywhere): star R=2, n=16384, FP64 storage, in(i,j)=i+j, out=0 -- the PRK
+stencil at 2.1 GB per array, the configuration the headline metric is quoted on. Every array is far
+larger than the 129 MB L2, so no flush is needed between steps. The same workload is also measured
+in the FP32-compensated form (the "fp32c" key) with its relative error against the FP64 oracle.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference's CPU implementation of the path (the OpenMP stencil, here as
+the oracle's port compiled with the reference's flags) on the host cores, same metric and config.
+With N > 1 (torchrun), each rank runs an independent replica of the workload (the stencil path has
+no exchange step on one grid per GPU); value is the sum over ranks, timed by the slowest rank.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "GFLOP/s + HBM GB/s, star R=2 n=16384: FP64 vs FP32-comp (rel err<=1e-6)"
+N_DEFAULT, R_DEFAULT = 16384, 2
+PEAK_FALLBACK_GBS = 6800.0
+
+
+def algorithmic_bytes(n: int, r: int, fp64: bool) -> float:
+    """Bytes one fused application must move: in read + in_next write over n^2, out read + write
+    over the interior. FP64: 16 n^2 + 16 (n-2R)^2. FP32C: 8 n^2 + 16 (n-2R)^2."""
+    return (16.0 if fp64 else 8.0) * n * n + 16.0 * (n - 2 * r) ** 2
+
+
+def hbm_peak() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return PEAK_FALLBACK_GBS, "fallback"
+
+
+def profiled_traffic() -> dict:
+    """DRAM bytes per launch from the committed ncu capture summary, if present."""
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            return {}
+    return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        mhz, maxmhz, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                mhz.append(float(f[1]))
+                maxmhz = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(mhz) if mhz else None, "sm_max_mhz": maxmhz,
+                "reasons": sorted(reasons), "samples": len(mhz)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_port_rate(pattern: int, r: int, n: int, applications: int, threads: int | None = None) -> dict:
+    """GFLOP/s of the CPU port (oracle compiled with the reference's -O3 -ffast-math -fopenmp) over
+    `applications` applications at size n, on all host cores unless `threads` is given."""
+    import numpy as np
+    from oracle import prk_oracle as po
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    lib = po.cpu_baseline()
+    a = np.empty((n, n))
+    o = np.empty((n, n))
+    lib.prk_oracle_init(n, 32, a.ctypes.data, o.ctypes.data)
+    lib.prk_oracle_sample(pattern, r, n, 1, 32, a.ctypes.data, o.ctypes.data)  # warm-up (first touch)
+    t = lib.prk_oracle_sample(pattern, r, n, applications, 32, a.ctypes.data, o.ctypes.data)
+    fl = po.flops(pattern, r, n)
+    return {"gflops": fl * applications / t / 1e9, "seconds": t, "threads": int(lib.prk_oracle_threads()),
+            "gbs": algorithmic_bytes(n, r, True) * applications / t / 1e9}
+
+
+def run_reference(args) -> None:
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    from oracle import prk_oracle as po
+    import numpy as np
+    n, r, pattern = args.n, args.radius, 0
+    lib = po.cpu_baseline()
+    a = np.empty((n, n))
+    o = np.empty((n, n))
+    lib.prk_oracle_init(n, 32, a.ctypes.data, o.ctypes.data)
+    lib.prk_oracle_sample(pattern, r, n, max(args.warmup, 1), 32, a.ctypes.data, o.ctypes.data)
+    t = lib.prk_oracle_sample(pattern, r, n, args.steps, 32, a.ctypes.data, o.ctypes.data)
+    fl = po.flops(pattern, r, n)
+    value = fl * args.steps / t / 1e9
+    threads = int(lib.prk_oracle_threads())
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * t / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"PRK star stencil R={r}, n={n}, FP64, one application + in+=1 per step",
+                   "pattern": "star", "radius": r, "n": n, "l2": "inputs larger than L2"},
+        "hbm_gbs": round(algorithmic_bytes(n, r, True) * args.steps / t / 1e9, 2),
+        "cpu_baseline": {"value": round(value, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} applications at n={n} (stencil-openmp loop restated in C, "
+                                   f"-O3 -ffast-math -fopenmp, OMP_NUM_THREADS={threads})"},
+        "e2e": {"value": round(value, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def time_steps(torch, kg, pattern, r, bufs, out, steps, warmup, stream) -> tuple[float, int]:
+    """W untimed + K timed fused applications on `stream`; returns (seconds, final parity)."""
+    cur = 0
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            kg.apply(pattern, r, bufs[cur], out, in_next=bufs[cur ^ 1], stream=stream)
+            cur ^= 1
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        stream.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            kg.apply(pattern, r, bufs[cur], out, in_next=bufs[cur ^ 1], stream=stream)
+            cur ^= 1
+        e1.record(stream)
+        e1.synchronize()
+    return e0.elapsed_time(e1) * 1e-3, cur
+
+
+def run_gb300(args) -> None:
+    import numpy as np
+    import torch
+    import kernels_gb300 as kg
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    n, r, pattern = args.n, args.radius, kg.STAR
+    stream = torch.cuda.Stream()
+    fl = kg.flops(pattern, r, n)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- FP64 (headline) ----
+    in_a, in_b, out = kg.alloc(n, kg.FP64)
+    kg.init(in_a, out)
+    barrier()
+    with ClockSampler(local) as clocks:
+        t64, cur = time_steps(torch, kg, pattern, r, (in_a, in_b), out, args.steps, args.warmup, stream)
+        barrier()
+    t64 = max_over_ranks(t64)
+    apps = args.steps + args.warmup
+    nrm = kg.norm(r, out)
+    norm_ok = abs(nrm - 2.0 * apps) <= 1e-8  # apps applications ran: norm = 2 * apps
+    del in_a, in_b, out
+    torch.cuda.empty_cache()
+
+    # ---- FP32C (the compensated form) on the same workload ----
+    in_a, in_b, out = kg.alloc(n, kg.FP32C)
+    kg.init(in_a, out)
+    barrier()
+    t32, _ = time_steps(torch, kg, pattern, r, (in_a, in_b), out, args.steps, args.warmup, stream)
+    barrier()
+    t32 = max_over_ranks(t32)
+    nrm32 = kg.norm(r, out)
+    from oracle import prk_oracle as po
+    rng = np.random.default_rng(3)
+    pts = [(int(i), int(j)) for i, j in rng.integers(r, n - r, (64, 2))]
+    idx = torch.tensor([i * n + j for i, j in pts], device="cuda")
+    o2 = out.reshape(-1, 2)[idx].double().cpu().numpy()
+    got = o2[:, 0] + o2[:, 1]
+    ref = np.array([po.point(pattern, r, n, apps, i, j) for i, j in pts])
+    rel32 = float(np.max(np.abs(got - ref) / np.abs(ref)))
+    del in_a, in_b, out
+    torch.cuda.empty_cache()
+
+    # ---- end to end through the host-buffer C-ABI call (copies inside the timed region) ----
+    e2e = None
+    if not args.no_e2e:
+        e2e_iters = args.e2e_iterations
+        h_in = torch.empty((n, n), dtype=torch.float64).pin_memory()
+        h_out = torch.zeros((n, n), dtype=torch.float64).pin_memory()
+        h_in.copy_(torch.arange(n, dtype=torch.float64)[:, None] + torch.arange(n, dtype=torch.float64)[None, :])
+        kg.run_host(pattern, r, 1, h_in, h_out)  # warm-up call (allocator, module load)
+        h_out.zero_()
+        barrier()
+        t0 = time.perf_counter()
+        res = kg.run_host(pattern, r, e2e_iters, h_in, h_out)
+        te = max_over_ranks(time.perf_counter() - t0)
+        e2e = {"value": round(world * fl * (e2e_iters + 1) / te / 1e9, 3), "unit": "GFLOP/s",
+               "h2d_bytes_per_step": 2 * n * n * 8, "d2h_bytes_per_step": n * n * 8 + 8,
+               "step": f"one prk_gb300_run_host call from pinned host buffers: copy in and out to the "
+                       f"device, {e2e_iters + 1} fused applications, copy out back, device norm",
+               "seconds": round(te, 4), "norm_ok": abs(res["norm"] - 2.0 * (e2e_iters + 1)) <= 1e-8}
+
+    peak, peak_kind = hbm_peak()
+    b64 = algorithmic_bytes(n, r, True)
+    b32 = algorithmic_bytes(n, r, False)
+    ach64 = b64 * args.steps / t64 / 1e9
+    ach32 = b32 * args.steps / t32 / 1e9
+    traffic = profiled_traffic().get("fp64_star2_n16384_bytes_per_launch")
+    value = world * fl * args.steps / t64 / 1e9
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1e3 * t64 / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"PRK star stencil R={r}, n={n}, FP64, one fused application (out += S(in), "
+                               f"in_next = in + 1) per step", "pattern": "star", "radius": r, "n": n,
+                   "l2": "inputs larger than L2 (2.1 GB per array), no flush", "parallelism": f"replicas x{world}"},
+        "hbm_gbs": round(world * ach64, 2),
+        "norm_check": norm_ok,
+        "roofline": {"bound": "hbm", "achieved": round(ach64, 2), "peak": peak, "unit": "GB/s",
+                     "frac": round(ach64 / peak, 4), "peak_source": peak_kind,
+                     "traffic": traffic, "algorithmic_bytes_per_launch": b64},
+        "fp32c": {"value": round(world * fl * args.steps / t32 / 1e9, 3), "unit": "GFLOP/s",
+                  "ms_per_step": round(1e3 * t32 / args.steps, 4), "hbm_gbs": round(ach32, 2),
+                  "roofline_frac": round(ach32 / peak, 4), "rel_err_vs_fp64_oracle": rel32,
+                  "norm_check": abs(nrm32 - 2.0 * apps) <= 1e-8, "algorithmic_bytes_per_launch": b32},
+        "clocks": clocks.summary(),
+        "gpu_launches": args.steps,
+    }
+    if e2e:
+        line["e2e"] = e2e
+    if rank == 0 and not args.no_cpu_baseline:
+        cb = cpu_port_rate(pattern, r, n, args.cpu_applications)
+        line["cpu_baseline"] = {"value": round(cb["gflops"], 3), "unit": "GFLOP/s", "cores": cb["threads"],
+                                "kind": "port",
+                                "sample": f"{args.cpu_applications} applications of star R=2 at n={n} "
+                                          f"({cb['seconds']:.2f} s), stencil-openmp loop restated in C with "
+                                          f"-O3 -ffast-math -fopenmp"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--radius", type=int, default=R_DEFAULT)
+    ap.add_argument("--e2e-iterations", type=int, default=100)
+    ap.add_argument("--cpu-applications", type=int, default=3)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)  # at least 3 untimed warm-up steps
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

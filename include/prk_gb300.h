@@ -1,0 +1,110 @@
+/*
+ * prk_gb300.h - C ABI of the GB300 (sm_103a) PRK 2D stencil library, libprk_gb300.so.
+ *
+ * The library replaces the stencil hot path of the Parallel Research Kernels' C++11 drivers
+ * (paths below are within the ParRes/Kernels project):
+ *
+ *   Cxx11/stencil_openmp.hpp:1       void starR/gridR(const int n, const int t, const double* in, double* out)
+ *   Cxx11/stencil_cuda.hpp:1         __global__ void starR/gridR(const int n, const prk_float* in, prk_float* out)
+ *   Cxx11/stencil-openmp.cc:208-218  the in += 1.0 sweep after each application
+ *   Cxx11/stencil-cuda.cu:76-84      __global__ void add(const int n, prk_float* in)
+ *   Cxx11/stencil-openmp.cc:230-239  L1 norm of out over the interior, divided by (n-2R)^2
+ *   Cxx11/stencil-openmp.cc:182-223  the driver's init and timed iteration loop
+ *
+ * Conventions shared by every entry point:
+ *   - Arrays are row-major n x n, element (i,j) at i*n+j, indices 64-bit (n is not capped at
+ *     46340 as prk::get_max_matrix_size() caps it, Cxx11/prk_util.h:373-377).
+ *   - Device pointers are owned by the caller (cudaMalloc alignment, 256 B, gives the fast path;
+ *     any 8-byte-aligned pointer works). The library allocates only where an entry point says so.
+ *   - dtype PRK_FP64: in, in_next, out are double[n*n].
+ *     dtype PRK_FP32C: in, in_next are float[n*n]; out is float[2*n*n], interleaved (hi, lo) pairs
+ *     whose unevaluated sum hi+lo is the value (a compensated two-float accumulator).
+ *   - stream is a cudaStream_t passed as void* (NULL = the legacy default stream). Calls are
+ *     stream-ordered and asynchronous unless stated otherwise. Calls on one stream from one host
+ *     thread at a time.
+ *   - Return value: 0 on success; a negative PRK_ERR_* code for a rejected call (nothing was
+ *     launched); a positive cudaError_t value when the CUDA runtime failed. The library never
+ *     aborts the process; prk_gb300_last_error() gives the message of the calling thread's last
+ *     failure.
+ */
+#ifndef PRK_GB300_H
+#define PRK_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PRK_STAR 0
+#define PRK_GRID 1
+
+#define PRK_FP64 0
+#define PRK_FP32C 1
+
+#define PRK_OK 0
+#define PRK_ERR_ARG (-1)     /* bad pattern, radius, n, dtype, iteration count or pointer */
+#define PRK_ERR_NOMEM (-2)   /* a library-owned allocation failed */
+#define PRK_ERR_STATE (-3)   /* call out of order (e.g. batch not prepared) */
+#define PRK_ERR_TIMEOUT (-4) /* a bounded device-side wait gave up (batched queue) */
+#define PRK_ERR_LIMIT (-5)   /* a size is above a documented fixed maximum */
+
+/* Flags for prk_gb300_run(). */
+#define PRK_RUN_GRAPH 1   /* capture the timed iteration loop in a CUDA graph and replay it */
+#define PRK_RUN_UNFUSED 2 /* reference structure: stencil kernel, then a separate in += 1 pass */
+
+/* One application of the stencil (replaces starR/gridR, stencil_openmp.hpp:1, stencil_cuda.hpp:1):
+ *   out[i*n+j] += sum over taps of w * in[(i+dr)*n + (j+dc)]   for R <= i,j < n-R,
+ * evaluated in the generator's tap order (generate-cxx-stencil.py:15-38).
+ * With in_next != NULL it also writes in_next = in + 1 over all n*n points (the fused form of the
+ * sweep at stencil-openmp.cc:208-218); in_next must not overlap in or out.
+ * With in_next == NULL it is exactly the reference operator: out is updated, in is untouched.
+ * PRK_FP64 results are bit-identical to the reference's strict-order binary64 evaluation. */
+int prk_gb300_stencil(int pattern, int radius, int64_t n, int dtype, const void* in, void* in_next, void* out,
+                      void* stream);
+
+/* in += 1 over all n*n points in place (stencil-openmp.cc:208-218, stencil-cuda.cu:76-84). */
+int prk_gb300_add(int64_t n, int dtype, void* in, void* stream);
+
+/* The drivers' initialisation (stencil-openmp.cc:184-195): in(i,j) = i+j, out = 0. */
+int prk_gb300_init(int64_t n, int dtype, void* in, void* out, void* stream);
+
+/* L1 norm of out over the interior divided by (n-2R)^2 (stencil-openmp.cc:230-239), reduced on
+ * the device in binary64 with a fixed order. Synchronous: waits for the stream and writes *norm.
+ * Uses a library-owned device scratch buffer, allocated once per device on first use. */
+int prk_gb300_norm(int radius, int64_t n, int dtype, const void* out, double* norm, void* stream);
+
+/* A whole PRK run on caller-owned device buffers (stencil-openmp.cc:197-223 / stencil-cuda.cu:211-222):
+ * iterations+1 applications, each followed by the in += 1 sweep; iteration 0 is the untimed warm-up
+ * and *elapsed_s receives the time of iterations 1..K measured with CUDA events on `stream`.
+ * The fused form ping-pongs between in_a (holding the initial in) and in_b; *final_in is set to 0
+ * or 1 for the buffer that holds the final in. With PRK_RUN_UNFUSED, in_b may be NULL and in_a is
+ * updated in place. Synchronous. */
+int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations, void* in_a, void* in_b, void* out,
+                  int flags, double* elapsed_s, int* final_in, void* stream);
+
+/* A whole PRK run from host memory, the way Cxx11/stencil-cuda.cu drives it (:193-226): copies
+ * h_in and h_out to the device, runs iterations+1 fused applications, copies out (and the final in,
+ * when h_in_final != NULL) back, and computes the norm. Allocates and frees its device buffers.
+ * *elapsed_s (optional) is the whole call's wall time including the copies; *kernel_s (optional)
+ * the event time of iterations 1..K. Host buffers may be pageable or pinned. */
+int prk_gb300_run_host(int pattern, int radius, int64_t n, int dtype, int iterations, const void* h_in, void* h_out,
+                       void* h_in_final, double* norm, double* elapsed_s, double* kernel_s);
+
+/* Bytes one buffer of the given role needs: role 0 = in / in_next, role 1 = out. */
+int64_t prk_gb300_bytes(int64_t n, int dtype, int role);
+
+/* PRK's flop count for one application, (2*stencil_size+1)*(n-2R)^2 (stencil-openmp.cc:253-255). */
+double prk_gb300_flops(int pattern, int radius, int64_t n);
+
+/* Message of the calling thread's last failed call ("" when none). */
+const char* prk_gb300_last_error(void);
+
+/* Library version string. */
+const char* prk_gb300_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PRK_GB300_H */

@@ -1,0 +1,169 @@
+"""kernels_gb300: the PRK 2D stencil hot path on GB300 (sm_103a).
+
+Host-side mirror of the reference operator interface over the C ABI (include/prk_gb300.h):
+
+  star1..star5, grid1..grid5(n, t, in_, out)
+      the reference operators' names and argument order (Cxx11/stencil_openmp.hpp:1,
+      Cxx11/stencil_cuda.hpp:1): out += S(in) over the interior, in untouched. `t` (the CPU tile) is
+      accepted and ignored.
+  apply(pattern, radius, in_, out, in_next=None)
+      one application; with in_next it also writes in_next = in + 1 (the fused sweep).
+  add(in_)          in += 1 (Cxx11/stencil-openmp.cc:208-218)
+  init(in_, out)    in = i+j, out = 0 (Cxx11/stencil-openmp.cc:184-195)
+  norm(radius, out) interior L1 norm / (n-2R)^2 (Cxx11/stencil-openmp.cc:230-239)
+  run(...)          a timed PRK run on device buffers (Cxx11/stencil-openmp.cc:197-223)
+  run_host(...)     a PRK run from host arrays, copies included (Cxx11/stencil-cuda.cu:193-226)
+
+Buffers are torch CUDA tensors (torch supplies device memory and streams only):
+  FP64:  in_/in_next float64 [n, n]; out float64 [n, n]
+  FP32C: in_/in_next float32 [n, n]; out float32 [n, n, 2] holding (hi, lo) pairs
+Every call raises PrkError on failure, with the library's message; arguments the reference rejects
+(radius outside 1..5, 2R+1 > n, iterations < 1) are rejected the same way.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+from ._lib import PrkError, check, load
+
+STAR, GRID = 0, 1
+FP64, FP32C = 0, 1
+RUN_GRAPH, RUN_UNFUSED = 1, 2
+
+__all__ = ["STAR", "GRID", "FP64", "FP32C", "PrkError", "apply", "add", "init", "norm", "run", "run_host",
+           "alloc", "flops", "pattern_of", "dtype_of", "version"] + \
+          [f"{p}{r}" for p in ("star", "grid") for r in range(1, 6)]
+
+
+def pattern_of(name: str) -> int:
+    """The reference's rule (stencil-openmp.cc:124-128): "grid" selects grid, anything else star."""
+    return GRID if name == "grid" else STAR
+
+
+def dtype_of(t) -> int:
+    import torch
+    if t.dtype == torch.float64:
+        return FP64
+    if t.dtype == torch.float32:
+        return FP32C
+    raise PrkError(-1, f"unsupported tensor dtype {t.dtype}: use float64 (fp64) or float32 (fp32c)")
+
+
+def _stream(stream) -> int | None:
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    return int(stream) if not hasattr(stream, "cuda_stream") else stream.cuda_stream
+
+
+def _n_of(in_) -> int:
+    if in_.dim() != 2 or in_.shape[0] != in_.shape[1] or not in_.is_contiguous():
+        raise PrkError(-1, "in must be a contiguous square [n, n] tensor")
+    return int(in_.shape[0])
+
+
+def _check_out(out, n: int, dtype: int) -> None:
+    import torch
+    want = (n, n) if dtype == FP64 else (n, n, 2)
+    wdt = torch.float64 if dtype == FP64 else torch.float32
+    if tuple(out.shape) != want or out.dtype != wdt or not out.is_contiguous():
+        raise PrkError(-1, f"out must be a contiguous {wdt} tensor of shape {want}")
+
+
+def version() -> str:
+    return load().prk_gb300_version().decode()
+
+
+def flops(pattern: int, radius: int, n: int) -> float:
+    """PRK's flop count of one application, (2*stencil_size+1)*(n-2R)^2."""
+    return float(load().prk_gb300_flops(pattern, radius, n))
+
+
+def apply(pattern: int, radius: int, in_, out, in_next=None, stream=None) -> None:
+    n = _n_of(in_)
+    dt = dtype_of(in_)
+    _check_out(out, n, dt)
+    if in_next is not None and (in_next.shape != in_.shape or in_next.dtype != in_.dtype or not in_next.is_contiguous()):
+        raise PrkError(-1, "in_next must match in")
+    check(load().prk_gb300_stencil(pattern, radius, n, dt, in_.data_ptr(), None if in_next is None else in_next.data_ptr(),
+                                   out.data_ptr(), _stream(stream)))
+
+
+def _make_op(pattern: int, radius: int):
+    def op(n: int, t: int, in_, out) -> None:
+        if _n_of(in_) != n:
+            raise PrkError(-1, f"n={n} does not match the tensor's {tuple(in_.shape)}")
+        apply(pattern, radius, in_, out)
+    op.__name__ = f"{'star' if pattern == STAR else 'grid'}{radius}"
+    op.__doc__ = f"Reference operator {op.__name__}(n, t, in, out): out += S(in) over the interior."
+    return op
+
+
+star1, star2, star3, star4, star5 = (_make_op(STAR, r) for r in range(1, 6))
+grid1, grid2, grid3, grid4, grid5 = (_make_op(GRID, r) for r in range(1, 6))
+
+
+def add(in_, stream=None) -> None:
+    check(load().prk_gb300_add(_n_of(in_), dtype_of(in_), in_.data_ptr(), _stream(stream)))
+
+
+def init(in_, out, stream=None) -> None:
+    n = _n_of(in_)
+    dt = dtype_of(in_)
+    _check_out(out, n, dt)
+    check(load().prk_gb300_init(n, dt, in_.data_ptr(), out.data_ptr(), _stream(stream)))
+
+
+def norm(radius: int, out, stream=None) -> float:
+    import torch
+    dt = FP64 if out.dtype == torch.float64 else FP32C
+    n = int(out.shape[0])
+    _check_out(out, n, dt)
+    res = C.c_double()
+    check(load().prk_gb300_norm(radius, n, dt, out.data_ptr(), C.byref(res), _stream(stream)))
+    return res.value
+
+
+@dataclass
+class RunResult:
+    elapsed_s: float   # event time of iterations 1..K
+    final_in: object   # the tensor that holds the final `in`
+
+
+def run(pattern: int, radius: int, iterations: int, in_a, in_b, out, graph: bool = False, unfused: bool = False,
+        stream=None) -> RunResult:
+    n = _n_of(in_a)
+    dt = dtype_of(in_a)
+    _check_out(out, n, dt)
+    el = C.c_double()
+    fin = C.c_int()
+    flags = (RUN_GRAPH if graph else 0) | (RUN_UNFUSED if unfused else 0)
+    check(load().prk_gb300_run(pattern, radius, n, dt, iterations, in_a.data_ptr(),
+                               None if in_b is None else in_b.data_ptr(), out.data_ptr(), flags, C.byref(el),
+                               C.byref(fin), _stream(stream)))
+    return RunResult(el.value, in_a if fin.value == 0 else in_b)
+
+
+def run_host(pattern: int, radius: int, iterations: int, h_in, h_out, h_in_final=None) -> dict:
+    """A whole run from host arrays (numpy or CPU tensors); returns norm and timings."""
+    def ptr(a):
+        return a.ctypes.data if hasattr(a, "ctypes") else a.data_ptr()
+    n = int(h_in.shape[0])
+    import numpy as np
+    dt = FP64 if h_in.dtype in (np.float64,) or str(h_in.dtype).endswith("float64") else FP32C
+    nrm, el, ks = C.c_double(), C.c_double(), C.c_double()
+    check(load().prk_gb300_run_host(pattern, radius, n, dt, iterations, ptr(h_in), ptr(h_out),
+                                    None if h_in_final is None else ptr(h_in_final), C.byref(nrm), C.byref(el),
+                                    C.byref(ks)))
+    return {"norm": nrm.value, "elapsed_s": el.value, "kernel_s": ks.value}
+
+
+def alloc(n: int, dtype: int = FP64, device="cuda", ping_pong: bool = True):
+    """Device buffers for a run: (in_a, in_b or None, out), uninitialised."""
+    import torch
+    tdt = torch.float64 if dtype == FP64 else torch.float32
+    in_a = torch.empty((n, n), dtype=tdt, device=device)
+    in_b = torch.empty((n, n), dtype=tdt, device=device) if ping_pong else None
+    out = torch.empty((n, n) if dtype == FP64 else (n, n, 2), dtype=tdt, device=device)
+    return in_a, in_b, out

@@ -1,0 +1,275 @@
+// C ABI of libprk_gb300.so (declared in include/prk_gb300.h): argument checks, dispatch to the
+// kernel launchers, the timed iteration loop and the host-buffer entry point. Errors are returned,
+// never raised: a negative PRK_ERR_* for a rejected call, a positive cudaError_t otherwise.
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/prk_gb300.h"
+#include "prk_internal.cuh"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what)
+{
+    return fail(static_cast<int>(e), "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+#define PRK_CUDA(call, what)                              \
+    do {                                                  \
+        cudaError_t e_ = (call);                          \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+int check_common(int radius, int64_t n, int dtype)
+{
+    if (dtype != PRK_FP64 && dtype != PRK_FP32C) return fail(PRK_ERR_ARG, "dtype %d is not PRK_FP64 or PRK_FP32C", dtype);
+    if (n < 1) return fail(PRK_ERR_ARG, "grid dimension must be positive (n=%lld)", static_cast<long long>(n));
+    if (n > prk::NMAX) return fail(PRK_ERR_LIMIT, "grid dimension %lld above the maximum %lld", static_cast<long long>(n),
+                                   static_cast<long long>(prk::NMAX));
+    if (radius < 1 || radius > prk::RMAX || 2 * static_cast<int64_t>(radius) + 1 > n)
+        return fail(PRK_ERR_ARG, "stencil radius %d negative or too large for n=%lld (1 <= R <= 5, 2R+1 <= n)", radius,
+                    static_cast<long long>(n));
+    return PRK_OK;
+}
+
+int check_stencil(int pattern, int radius, int64_t n, int dtype)
+{
+    if (pattern != PRK_STAR && pattern != PRK_GRID) return fail(PRK_ERR_ARG, "pattern %d is not PRK_STAR or PRK_GRID", pattern);
+    return check_common(radius, n, dtype);
+}
+
+bool overlaps(const void* a, int64_t abytes, const void* b, int64_t bbytes)
+{
+    const char* pa = static_cast<const char*>(a);
+    const char* pb = static_cast<const char*>(b);
+    return pa < pb + bbytes && pb < pa + abytes;
+}
+
+// Library-owned device scratch for the norm: NORM_BLOCKS partial sums and the result, one
+// allocation per device, kept until the process exits.
+struct NormScratch {
+    double* dev = nullptr;
+};
+std::mutex g_scratch_mu;
+std::vector<NormScratch> g_scratch;
+
+int norm_scratch(double** out)
+{
+    int dev = 0;
+    PRK_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (static_cast<int>(g_scratch.size()) <= dev) g_scratch.resize(dev + 1);
+    if (!g_scratch[dev].dev) {
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, (prk::NORM_BLOCKS + 1) * sizeof(double));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(PRK_ERR_NOMEM, "cudaMalloc of the norm scratch failed: %s", cudaGetErrorString(e));
+        }
+        g_scratch[dev].dev = static_cast<double*>(p);
+    }
+    *out = g_scratch[dev].dev;
+    return PRK_OK;
+}
+
+int launch_one(int pattern, int radius, int64_t n, int dtype, const void* in, void* in_next, void* out, cudaStream_t s)
+{
+    prk::StencilCall c{pattern, radius, n, dtype, in, in_next, out, s};
+    PRK_CUDA(prk::launch_stencil_generic(c), "stencil launch");
+    return PRK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* prk_gb300_last_error(void) { return g_last_error.c_str(); }
+
+const char* prk_gb300_version(void) { return "prk_gb300 0.1.0 (sm_103a)"; }
+
+int64_t prk_gb300_bytes(int64_t n, int dtype, int role)
+{
+    if (n < 1 || (dtype != PRK_FP64 && dtype != PRK_FP32C)) return -1;
+    return n * n * (role == 0 ? prk::in_elem_bytes(dtype) : prk::out_elem_bytes(dtype));
+}
+
+double prk_gb300_flops(int pattern, int radius, int64_t n)
+{
+    const double act = static_cast<double>(n - 2 * radius) * static_cast<double>(n - 2 * radius);
+    return (2.0 * prk::stencil_size(pattern == PRK_GRID ? prk::GRID : prk::STAR, radius) + 1.0) * act;
+}
+
+int prk_gb300_stencil(int pattern, int radius, int64_t n, int dtype, const void* in, void* in_next, void* out, void* stream)
+{
+    if (int rc = check_stencil(pattern, radius, n, dtype)) return rc;
+    if (!in || !out) return fail(PRK_ERR_ARG, "in and out must be non-null device pointers");
+    const int64_t ib = prk_gb300_bytes(n, dtype, 0), ob = prk_gb300_bytes(n, dtype, 1);
+    if (overlaps(in, ib, out, ob)) return fail(PRK_ERR_ARG, "in and out overlap");
+    if (in_next && (overlaps(in_next, ib, in, ib) || overlaps(in_next, ib, out, ob)))
+        return fail(PRK_ERR_ARG, "in_next overlaps in or out");
+    return launch_one(pattern, radius, n, dtype, in, in_next, out, static_cast<cudaStream_t>(stream));
+}
+
+int prk_gb300_add(int64_t n, int dtype, void* in, void* stream)
+{
+    if (dtype != PRK_FP64 && dtype != PRK_FP32C) return fail(PRK_ERR_ARG, "dtype %d is not PRK_FP64 or PRK_FP32C", dtype);
+    if (n < 1 || !in) return fail(PRK_ERR_ARG, "n must be positive and in non-null");
+    PRK_CUDA(prk::launch_add(n, dtype, in, static_cast<cudaStream_t>(stream)), "add launch");
+    return PRK_OK;
+}
+
+int prk_gb300_init(int64_t n, int dtype, void* in, void* out, void* stream)
+{
+    if (dtype != PRK_FP64 && dtype != PRK_FP32C) return fail(PRK_ERR_ARG, "dtype %d is not PRK_FP64 or PRK_FP32C", dtype);
+    if (n < 1 || !in || !out) return fail(PRK_ERR_ARG, "n must be positive and in, out non-null");
+    PRK_CUDA(prk::launch_init(n, dtype, in, out, static_cast<cudaStream_t>(stream)), "init launch");
+    return PRK_OK;
+}
+
+int prk_gb300_norm(int radius, int64_t n, int dtype, const void* out, double* norm, void* stream)
+{
+    if (int rc = check_common(radius, n, dtype)) return rc;
+    if (!out || !norm) return fail(PRK_ERR_ARG, "out and norm must be non-null");
+    double* scratch = nullptr;
+    if (int rc = norm_scratch(&scratch)) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    PRK_CUDA(prk::launch_norm(radius, n, dtype, out, scratch, scratch + prk::NORM_BLOCKS, s), "norm launch");
+    PRK_CUDA(cudaMemcpyAsync(norm, scratch + prk::NORM_BLOCKS, sizeof(double), cudaMemcpyDeviceToHost, s), "norm copy");
+    PRK_CUDA(cudaStreamSynchronize(s), "norm synchronize");
+    return PRK_OK;
+}
+
+int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations, void* in_a, void* in_b, void* out,
+                  int flags, double* elapsed_s, int* final_in, void* stream)
+{
+    if (int rc = check_stencil(pattern, radius, n, dtype)) return rc;
+    if (iterations < 1) return fail(PRK_ERR_ARG, "iterations must be >= 1");
+    const bool unfused = (flags & PRK_RUN_UNFUSED) != 0;
+    const bool graph = (flags & PRK_RUN_GRAPH) != 0;
+    if (!in_a || !out || (!unfused && !in_b)) return fail(PRK_ERR_ARG, "null buffer");
+    const int64_t ib = prk_gb300_bytes(n, dtype, 0), ob = prk_gb300_bytes(n, dtype, 1);
+    if (overlaps(in_a, ib, out, ob) || (!unfused && (overlaps(in_b, ib, out, ob) || overlaps(in_a, ib, in_b, ib))))
+        return fail(PRK_ERR_ARG, "buffers overlap");
+
+    cudaStream_t user = static_cast<cudaStream_t>(stream);
+    cudaStream_t s = user;
+    cudaStream_t own = nullptr;
+    if (graph && s == nullptr) {  // capture needs a non-legacy stream
+        PRK_CUDA(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking), "cudaStreamCreate");
+        s = own;
+    }
+    void* bufs[2] = {in_a, in_b};
+    int cur = 0;
+    auto step = [&](cudaStream_t st) -> int {
+        if (unfused) {
+            if (int rc = launch_one(pattern, radius, n, dtype, in_a, nullptr, out, st)) return rc;
+            PRK_CUDA(prk::launch_add(n, dtype, in_a, st), "add launch");
+        } else {
+            if (int rc = launch_one(pattern, radius, n, dtype, bufs[cur], bufs[cur ^ 1], out, st)) return rc;
+            cur ^= 1;
+        }
+        return PRK_OK;
+    };
+
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    int rc = PRK_OK;
+    do {
+        cudaError_t ce;
+        if (own) {  // order the private stream after prior work on the legacy stream
+            cudaEvent_t dep;
+            if ((ce = cudaEventCreateWithFlags(&dep, cudaEventDisableTiming)) != cudaSuccess) { rc = cuda_fail(ce, "cudaEventCreate"); break; }
+            cudaEventRecord(dep, nullptr);
+            cudaStreamWaitEvent(s, dep, 0);
+            cudaEventDestroy(dep);
+        }
+        if ((ce = cudaEventCreate(&e0)) != cudaSuccess || (ce = cudaEventCreate(&e1)) != cudaSuccess) { rc = cuda_fail(ce, "cudaEventCreate"); break; }
+        if ((rc = step(s)) != PRK_OK) break;  // iteration 0: untimed warm-up
+        if (graph) {
+            if ((ce = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) { rc = cuda_fail(ce, "cudaStreamBeginCapture"); break; }
+            for (int it = 1; it <= iterations && rc == PRK_OK; ++it) rc = step(s);
+            cudaError_t ec = cudaStreamEndCapture(s, &g);
+            if (rc != PRK_OK) break;
+            if (ec != cudaSuccess) { rc = cuda_fail(ec, "cudaStreamEndCapture"); break; }
+            if ((ce = cudaGraphInstantiate(&ge, g, 0)) != cudaSuccess) { rc = cuda_fail(ce, "cudaGraphInstantiate"); break; }
+            if ((ce = cudaGraphUpload(ge, s)) != cudaSuccess) { rc = cuda_fail(ce, "cudaGraphUpload"); break; }
+            cudaEventRecord(e0, s);
+            if ((ce = cudaGraphLaunch(ge, s)) != cudaSuccess) { rc = cuda_fail(ce, "cudaGraphLaunch"); break; }
+            cudaEventRecord(e1, s);
+        } else {
+            cudaEventRecord(e0, s);
+            for (int it = 1; it <= iterations && rc == PRK_OK; ++it) rc = step(s);
+            if (rc != PRK_OK) break;
+            cudaEventRecord(e1, s);
+        }
+        if ((ce = cudaEventSynchronize(e1)) != cudaSuccess) { rc = cuda_fail(ce, "iteration loop"); break; }
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (elapsed_s) *elapsed_s = ms * 1e-3;
+        if (final_in) *final_in = unfused ? 0 : cur;
+    } while (false);
+    if (ge) cudaGraphExecDestroy(ge);
+    if (g) cudaGraphDestroy(g);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (own) {
+        cudaStreamSynchronize(own);
+        cudaStreamDestroy(own);
+    }
+    return rc;
+}
+
+int prk_gb300_run_host(int pattern, int radius, int64_t n, int dtype, int iterations, const void* h_in, void* h_out,
+                       void* h_in_final, double* norm, double* elapsed_s, double* kernel_s)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    if (int rc = check_stencil(pattern, radius, n, dtype)) return rc;
+    if (iterations < 1) return fail(PRK_ERR_ARG, "iterations must be >= 1");
+    if (!h_in || !h_out) return fail(PRK_ERR_ARG, "h_in and h_out must be non-null");
+    const int64_t ib = prk_gb300_bytes(n, dtype, 0), ob = prk_gb300_bytes(n, dtype, 1);
+    void* d[3] = {nullptr, nullptr, nullptr};
+    int rc = PRK_OK;
+    do {
+        cudaError_t ce;
+        if ((ce = cudaMalloc(&d[0], ib)) != cudaSuccess || (ce = cudaMalloc(&d[1], ib)) != cudaSuccess ||
+            (ce = cudaMalloc(&d[2], ob)) != cudaSuccess) {
+            cudaGetLastError();
+            rc = fail(PRK_ERR_NOMEM, "device allocation of %lld bytes failed: %s", static_cast<long long>(2 * ib + ob),
+                      cudaGetErrorString(ce));
+            break;
+        }
+        if ((ce = cudaMemcpy(d[0], h_in, ib, cudaMemcpyHostToDevice)) != cudaSuccess ||
+            (ce = cudaMemcpy(d[2], h_out, ob, cudaMemcpyHostToDevice)) != cudaSuccess) { rc = cuda_fail(ce, "host to device copy"); break; }
+        int fin = 0;
+        double ks = 0.0;
+        if ((rc = prk_gb300_run(pattern, radius, n, dtype, iterations, d[0], d[1], d[2], 0, &ks, &fin, nullptr)) != PRK_OK) break;
+        if ((ce = cudaMemcpy(h_out, d[2], ob, cudaMemcpyDeviceToHost)) != cudaSuccess) { rc = cuda_fail(ce, "device to host copy"); break; }
+        if (h_in_final && (ce = cudaMemcpy(h_in_final, d[fin], ib, cudaMemcpyDeviceToHost)) != cudaSuccess) { rc = cuda_fail(ce, "device to host copy"); break; }
+        if (norm && (rc = prk_gb300_norm(radius, n, dtype, d[2], norm, nullptr)) != PRK_OK) break;
+        if (kernel_s) *kernel_s = ks;
+    } while (false);
+    for (void* p : d)
+        if (p) cudaFree(p);
+    if (elapsed_s) *elapsed_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,39 @@
+// Internal launcher interface between the C ABI (capi.cu) and the kernel translation units.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "prk_stencil.cuh"
+
+namespace prk {
+
+// One stencil application as the C ABI describes it (prk_gb300_stencil).
+struct StencilCall {
+    int pattern;
+    int R;
+    int64_t n;
+    int dtype;
+    const void* in;
+    void* in_next;  // may be null: stencil only, in untouched
+    void* out;
+    cudaStream_t stream;
+};
+
+// Largest n the tile grids address (gridDim.y = ceil(n/16) <= 65535).
+constexpr int64_t NMAX = 65535LL * 16;
+
+// Bytes per point of one in buffer and of the out buffer.
+inline int64_t in_elem_bytes(int dtype) { return dtype == FP64 ? 8 : 4; }
+inline int64_t out_elem_bytes(int dtype) { return 8; }
+
+// kernels_generic.cu: any n, any 8-byte-aligned pointers.
+cudaError_t launch_stencil_generic(const StencilCall& c);
+cudaError_t launch_add(int64_t n, int dtype, void* in, cudaStream_t s);
+cudaError_t launch_init(int64_t n, int dtype, void* in, void* out, cudaStream_t s);
+// Writes the interior L1 norm / (n-2R)^2 to *result_dev; partial must hold NORM_BLOCKS doubles.
+constexpr int NORM_BLOCKS = 1024;
+cudaError_t launch_norm(int R, int64_t n, int dtype, const void* out, double* partial, double* result_dev,
+                        cudaStream_t s);
+
+}  // namespace prk
