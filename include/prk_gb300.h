@@ -91,6 +91,25 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
 int prk_gb300_run_host(int pattern, int radius, int64_t n, int dtype, int iterations, const void* h_in, void* h_out,
                        void* h_in_final, double* norm, double* elapsed_s, double* kernel_s);
 
+/* Capacity of the fixed scratch behind prk_gb300_norm_noalloc: partial sums, 8 KiB per device. */
+#define PRK_NOALLOC_NORM_PARTIALS 1024
+
+/* The L1 norm of prk_gb300_norm, for callers that cannot let the library allocate device memory
+ * (a framework whose caching allocator owns the device's memory, a service on a fixed memory
+ * budget, a loop that cannot afford cudaMalloc's implicit device synchronisation). No counterpart
+ * in the reference: the reference computes its norm on the host after copying out back.
+ * - Allocates nothing: no cudaMalloc, cudaFree or allocating library call. Its scratch is a fixed
+ *   array of PRK_NOALLOC_NORM_PARTIALS doubles inside the library's device image, held by every
+ *   device that loads the library until the process exits; a reduction that would need more
+ *   partial sums is rejected with PRK_ERR_LIMIT (with the norm's fixed block count, none does).
+ * - norm_dev is caller-owned DEVICE memory for one double; the result is the same value
+ *   prk_gb300_norm returns. Stream-ordered and asynchronous: read *norm_dev after the stream.
+ * - The first call on each device looks up the scratch's device address (cudaGetSymbolAddress)
+ *   with that device current; make that first call before any stream capture.
+ * - Every call shares the scratch, which keeps the last call's contents (nothing in it needs to
+ *   start at zero). Calls that overlap on the GPU, e.g. on two streams, race on it. */
+int prk_gb300_norm_noalloc(int radius, int64_t n, int dtype, const void* out, double* norm_dev, void* stream);
+
 /* Bytes one buffer of the given role needs: role 0 = in / in_next, role 1 = out. */
 int64_t prk_gb300_bytes(int64_t n, int dtype, int role);
 

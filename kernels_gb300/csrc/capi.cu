@@ -98,6 +98,8 @@ int launch_one(int pattern, int radius, int64_t n, int dtype, const void* in, vo
 
 }  // namespace
 
+int prk::record_error(int code, const char* msg) { return fail(code, "%s", msg); }
+
 extern "C" {
 
 const char* prk_gb300_last_error(void) { return g_last_error.c_str(); }

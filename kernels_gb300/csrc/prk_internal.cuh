@@ -36,4 +36,7 @@ constexpr int NORM_BLOCKS = 1024;
 cudaError_t launch_norm(int R, int64_t n, int dtype, const void* out, double* partial, double* result_dev,
                         cudaStream_t s);
 
+// Records `msg` as the calling thread's prk_gb300_last_error() and returns `code` (capi.cu).
+int record_error(int code, const char* msg);
+
 }  // namespace prk
