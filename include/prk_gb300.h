@@ -110,6 +110,18 @@ int prk_gb300_run_host(int pattern, int radius, int64_t n, int dtype, int iterat
  *   start at zero). Calls that overlap on the GPU, e.g. on two streams, race on it. */
 int prk_gb300_norm_noalloc(int radius, int64_t n, int dtype, const void* out, double* norm_dev, void* stream);
 
+/* Process-wide settings. PRK_CFG_KERNEL selects the stencil kernel family: 0 = automatic (the TMA
+ * tile kernels for the fused form on 16-byte-aligned buffers with n a multiple of 2 (FP64) or 4
+ * (FP32C), the generic kernels otherwise), 1 = generic kernels only, 2 = TMA kernels required (calls
+ * that are not eligible fail with PRK_ERR_ARG). Returns the previous value, or a negative error. */
+#define PRK_CFG_KERNEL 1
+int prk_gb300_config(int key, int value);
+
+/* Reads and clears the device status word of the current device: PRK_OK, or PRK_ERR_TIMEOUT when a
+ * kernel's bounded wait on its tile loads gave up since the last check. Synchronises the device.
+ * prk_gb300_run checks it after every run. */
+int prk_gb300_status(void);
+
 /* Bytes one buffer of the given role needs: role 0 = in / in_next, role 1 = out. */
 int64_t prk_gb300_bytes(int64_t n, int dtype, int role);
 

@@ -32,7 +32,8 @@ FP64, FP32C = 0, 1
 RUN_GRAPH, RUN_UNFUSED = 1, 2
 
 __all__ = ["STAR", "GRID", "FP64", "FP32C", "PrkError", "apply", "add", "init", "norm", "run", "run_host",
-           "alloc", "flops", "pattern_of", "dtype_of", "version"] + \
+           "alloc", "flops", "pattern_of", "dtype_of", "version", "set_kernel", "status", "KERNEL_AUTO",
+           "KERNEL_GENERIC", "KERNEL_TMA"] + \
           [f"{p}{r}" for p in ("star", "grid") for r in range(1, 6)]
 
 
@@ -69,6 +70,23 @@ def _check_out(out, n: int, dtype: int) -> None:
     wdt = torch.float64 if dtype == FP64 else torch.float32
     if tuple(out.shape) != want or out.dtype != wdt or not out.is_contiguous():
         raise PrkError(-1, f"out must be a contiguous {wdt} tensor of shape {want}")
+
+
+KERNEL_AUTO, KERNEL_GENERIC, KERNEL_TMA = 0, 1, 2
+
+
+def set_kernel(choice: int) -> int:
+    """Select the stencil kernel family process-wide (PRK_CFG_KERNEL): KERNEL_AUTO, KERNEL_GENERIC
+    or KERNEL_TMA. Returns the previous choice."""
+    rc = load().prk_gb300_config(1, choice)
+    if rc < 0:
+        check(rc)
+    return rc
+
+
+def status() -> None:
+    """Raise if a kernel's bounded wait gave up since the last check (synchronises the device)."""
+    check(load().prk_gb300_status())
 
 
 def version() -> str:

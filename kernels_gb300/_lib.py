@@ -30,6 +30,8 @@ SIGNATURES: dict[str, tuple] = {
     "prk_gb300_norm_noalloc": (_int, [_int, _i64, _int, _vp, _vp, _vp]),
     "prk_gb300_run": (_int, [_int, _int, _i64, _int, _int, _vp, _vp, _vp, _int, _pd, _pi, _vp]),
     "prk_gb300_run_host": (_int, [_int, _int, _i64, _int, _int, _vp, _vp, _vp, _pd, _pd, _pd]),
+    "prk_gb300_config": (_int, [_int, _int]),
+    "prk_gb300_status": (_int, []),
     "prk_gb300_bytes": (_i64, [_i64, _int, _int]),
     "prk_gb300_flops": (_dbl, [_int, _int, _i64]),
     "prk_gb300_last_error": (C.c_char_p, []),

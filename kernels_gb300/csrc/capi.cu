@@ -62,37 +62,76 @@ bool overlaps(const void* a, int64_t abytes, const void* b, int64_t bbytes)
     return pa < pb + bbytes && pb < pa + abytes;
 }
 
-// Library-owned device scratch for the norm: NORM_BLOCKS partial sums and the result, one
-// allocation per device, kept until the process exits.
-struct NormScratch {
-    double* dev = nullptr;
+// Library-owned device scratch: NORM_BLOCKS partial sums and the result for the norm, and the
+// status word the tile kernels set when a bounded wait gives up. One allocation per device, kept
+// until the process exits.
+struct DevScratch {
+    double* norm = nullptr;
+    unsigned* status = nullptr;
 };
 std::mutex g_scratch_mu;
-std::vector<NormScratch> g_scratch;
+std::vector<DevScratch> g_scratch;
 
-int norm_scratch(double** out)
+int dev_scratch(DevScratch* out)
 {
     int dev = 0;
     PRK_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
     std::lock_guard<std::mutex> lock(g_scratch_mu);
     if (static_cast<int>(g_scratch.size()) <= dev) g_scratch.resize(dev + 1);
-    if (!g_scratch[dev].dev) {
+    if (!g_scratch[dev].norm) {
         void* p = nullptr;
-        cudaError_t e = cudaMalloc(&p, (prk::NORM_BLOCKS + 1) * sizeof(double));
+        const size_t bytes = (prk::NORM_BLOCKS + 1) * sizeof(double) + 256;
+        cudaError_t e = cudaMalloc(&p, bytes);
         if (e != cudaSuccess) {
             cudaGetLastError();
-            return fail(PRK_ERR_NOMEM, "cudaMalloc of the norm scratch failed: %s", cudaGetErrorString(e));
+            return fail(PRK_ERR_NOMEM, "cudaMalloc of the library scratch failed: %s", cudaGetErrorString(e));
         }
-        g_scratch[dev].dev = static_cast<double*>(p);
+        e = cudaMemset(p, 0, bytes);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemset of the library scratch");
+        g_scratch[dev].norm = static_cast<double*>(p);
+        g_scratch[dev].status = reinterpret_cast<unsigned*>(static_cast<char*>(p) + (prk::NORM_BLOCKS + 1) * sizeof(double));
     }
-    *out = g_scratch[dev].dev;
+    *out = g_scratch[dev];
     return PRK_OK;
 }
+
+int norm_scratch(double** out)
+{
+    DevScratch d;
+    if (int rc = dev_scratch(&d)) return rc;
+    *out = d.norm;
+    return PRK_OK;
+}
+
+// Kernel selection: 0 = automatic (TMA tiles where eligible), 1 = generic only, 2 = TMA required.
+int g_kernel_choice = 0;
 
 int launch_one(int pattern, int radius, int64_t n, int dtype, const void* in, void* in_next, void* out, cudaStream_t s)
 {
     prk::StencilCall c{pattern, radius, n, dtype, in, in_next, out, s};
-    PRK_CUDA(prk::launch_stencil_generic(c), "stencil launch");
+    const bool tma = g_kernel_choice != 1 && prk::tma_eligible(c);
+    if (g_kernel_choice == 2 && !tma) return fail(PRK_ERR_ARG, "the TMA tile kernel was required but the call is not eligible");
+    if (tma) {
+        DevScratch d;
+        if (int rc = dev_scratch(&d)) return rc;
+        PRK_CUDA(prk::launch_stencil_tma(c, d.status), "stencil launch (TMA tiles)");
+    } else {
+        PRK_CUDA(prk::launch_stencil_generic(c), "stencil launch");
+    }
+    return PRK_OK;
+}
+
+// Reads and clears the device status word (synchronises the device).
+int check_status()
+{
+    DevScratch d;
+    if (int rc = dev_scratch(&d)) return rc;
+    unsigned st = 0;
+    PRK_CUDA(cudaMemcpy(&st, d.status, sizeof st, cudaMemcpyDeviceToHost), "status read");
+    if (st) {
+        PRK_CUDA(cudaMemset(d.status, 0, sizeof st), "status clear");
+        return fail(PRK_ERR_TIMEOUT, "a bounded device-side wait gave up (status 0x%x)", st);
+    }
     return PRK_OK;
 }
 
@@ -104,7 +143,20 @@ extern "C" {
 
 const char* prk_gb300_last_error(void) { return g_last_error.c_str(); }
 
-const char* prk_gb300_version(void) { return "prk_gb300 0.1.0 (sm_103a)"; }
+const char* prk_gb300_version(void) { return "prk_gb300 0.2.0 (sm_103a)"; }
+
+int prk_gb300_config(int key, int value)
+{
+    if (key == PRK_CFG_KERNEL) {
+        if (value < 0 || value > 2) return fail(PRK_ERR_ARG, "PRK_CFG_KERNEL takes 0 (auto), 1 (generic) or 2 (TMA)");
+        const int old = g_kernel_choice;
+        g_kernel_choice = value;
+        return old;
+    }
+    return fail(PRK_ERR_ARG, "unknown configuration key %d", key);
+}
+
+int prk_gb300_status(void) { return check_status(); }
 
 int64_t prk_gb300_bytes(int64_t n, int dtype, int role)
 {
@@ -227,6 +279,7 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
         cudaEventElapsedTime(&ms, e0, e1);
         if (elapsed_s) *elapsed_s = ms * 1e-3;
         if (final_in) *final_in = unfused ? 0 : cur;
+        rc = check_status();
     } while (false);
     if (ge) cudaGraphExecDestroy(ge);
     if (g) cudaGraphDestroy(g);
