@@ -189,6 +189,25 @@ def time_steps(torch, kg, pattern, r, bufs, out, steps, warmup, stream) -> tuple
     return e0.elapsed_time(e1) * 1e-3, cur
 
 
+def time_depth(torch, kg, pattern, r, bufs, out, apps, depth, stream) -> float:
+    """`apps` applications as apps/depth launches of `depth` applications each; returns seconds."""
+    cur = 0
+    with torch.cuda.stream(stream):
+        for _ in range(3):  # warm-up launches
+            kg.apply_steps(pattern, r, depth, bufs[cur], out, bufs[cur ^ 1], stream=stream)
+            cur ^= 1
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        stream.synchronize()
+        e0.record(stream)
+        for _ in range(apps // depth):
+            kg.apply_steps(pattern, r, depth, bufs[cur], out, bufs[cur ^ 1], stream=stream)
+            cur ^= 1
+        e1.record(stream)
+        e1.synchronize()
+    return e0.elapsed_time(e1) * 1e-3
+
+
 def run_gb300(args) -> None:
     import numpy as np
     import torch
@@ -227,6 +246,12 @@ def run_gb300(args) -> None:
     apps = args.steps + args.warmup
     nrm = kg.norm(r, out)
     norm_ok = abs(nrm - 2.0 * apps) <= 1e-8  # apps applications ran: norm = 2 * apps
+    temporal = {"fp64": {}, "fp32c": {}}
+    if not args.no_temporal:
+        for depth in (2, 4, 8):
+            td = time_depth(torch, kg, pattern, r, (in_a, in_b), out, 8 * (args.steps // 8 or 1), depth, stream)
+            napps = 8 * (args.steps // 8 or 1)
+            temporal["fp64"][str(depth)] = round(fl * napps / td / 1e9, 3)
     del in_a, in_b, out
     torch.cuda.empty_cache()
 
@@ -246,6 +271,11 @@ def run_gb300(args) -> None:
     got = o2[:, 0] + o2[:, 1]
     ref = np.array([po.point(pattern, r, n, apps, i, j) for i, j in pts])
     rel32 = float(np.max(np.abs(got - ref) / np.abs(ref)))
+    if not args.no_temporal:
+        for depth in (2, 4, 8):
+            napps = 8 * (args.steps // 8 or 1)
+            td = time_depth(torch, kg, pattern, r, (in_a, in_b), out, napps, depth, stream)
+            temporal["fp32c"][str(depth)] = round(fl * napps / td / 1e9, 3)
     del in_a, in_b, out
     torch.cuda.empty_cache()
 
@@ -291,6 +321,9 @@ def run_gb300(args) -> None:
                   "ms_per_step": round(1e3 * t32 / args.steps, 4), "hbm_gbs": round(ach32, 2),
                   "roofline_frac": round(ach32 / peak, 4), "rel_err_vs_fp64_oracle": rel32,
                   "norm_check": abs(nrm32 - 2.0 * apps) <= 1e-8, "algorithmic_bytes_per_launch": b32},
+        "temporal": {"unit": "GFLOP/s", "what": "the same workload with `depth` applications per launch on a tile "
+                                                "held in shared memory (temporal blocking); keys are depths",
+                     **temporal} if not args.no_temporal else None,
         "clocks": clocks.summary(),
         "gpu_launches": args.steps,
     }
@@ -321,6 +354,7 @@ def main() -> None:
     ap.add_argument("--cpu-applications", type=int, default=3)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-temporal", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)  # at least 3 untimed warm-up steps
     if args.impl == "reference":

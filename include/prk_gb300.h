@@ -52,6 +52,9 @@ extern "C" {
 /* Flags for prk_gb300_run(). */
 #define PRK_RUN_GRAPH 1   /* capture the timed iteration loop in a CUDA graph and replay it */
 #define PRK_RUN_UNFUSED 2 /* reference structure: stencil kernel, then a separate in += 1 pass */
+/* Temporal depth d in {1, 2, 4, 8}: each launch applies d consecutive applications to a tile held
+ * in shared memory (the fused form on TMA-eligible buffers; otherwise depth 1). */
+#define PRK_RUN_DEPTH(d) ((d) << 8)
 
 /* One application of the stencil (replaces starR/gridR, stencil_openmp.hpp:1, stencil_cuda.hpp:1):
  *   out[i*n+j] += sum over taps of w * in[(i+dr)*n + (j+dc)]   for R <= i,j < n-R,
@@ -62,6 +65,16 @@ extern "C" {
  * PRK_FP64 results are bit-identical to the reference's strict-order binary64 evaluation. */
 int prk_gb300_stencil(int pattern, int radius, int64_t n, int dtype, const void* in, void* in_next, void* out,
                       void* stream);
+
+/* `steps` consecutive fused applications in one launch (temporal blocking), steps in {1, 2, 4, 8}:
+ * out += S(in) + S(in+1) + ... + S(in+steps-1) with out rounded after every application exactly as
+ * `steps` single applications round it, and in_next = in + steps (each +1 rounded in turn). Every
+ * application reads the in values and applies every tap; only the HBM round trips between them are
+ * saved. in is not modified. Needs 16-byte-aligned buffers and n a multiple of 2 (PRK_FP64) or 4
+ * (PRK_FP32C); otherwise PRK_ERR_ARG. No counterpart in the reference, whose loop always makes the
+ * round trip (Cxx11/stencil-openmp.cc:197-219). */
+int prk_gb300_stencil_steps(int pattern, int radius, int64_t n, int dtype, int steps, const void* in, void* in_next,
+                            void* out, void* stream);
 
 /* in += 1 over all n*n points in place (stencil-openmp.cc:208-218, stencil-cuda.cu:76-84). */
 int prk_gb300_add(int64_t n, int dtype, void* in, void* stream);

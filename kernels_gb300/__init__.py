@@ -32,7 +32,7 @@ FP64, FP32C = 0, 1
 RUN_GRAPH, RUN_UNFUSED = 1, 2
 
 __all__ = ["STAR", "GRID", "FP64", "FP32C", "PrkError", "apply", "add", "init", "norm", "run", "run_host",
-           "alloc", "flops", "pattern_of", "dtype_of", "version", "set_kernel", "status", "KERNEL_AUTO",
+           "alloc", "apply_steps", "flops", "pattern_of", "dtype_of", "version", "set_kernel", "status", "KERNEL_AUTO",
            "KERNEL_GENERIC", "KERNEL_TMA"] + \
           [f"{p}{r}" for p in ("star", "grid") for r in range(1, 6)]
 
@@ -108,6 +108,18 @@ def apply(pattern: int, radius: int, in_, out, in_next=None, stream=None) -> Non
                                    out.data_ptr(), _stream(stream)))
 
 
+def apply_steps(pattern: int, radius: int, steps: int, in_, out, in_next, stream=None) -> None:
+    """`steps` (1, 2, 4 or 8) fused applications in one launch: out accumulates every application,
+    in_next = in + steps. Requires the TMA-eligible layout (16-byte alignment, n % 2 or n % 4)."""
+    n = _n_of(in_)
+    dt = dtype_of(in_)
+    _check_out(out, n, dt)
+    if in_next.shape != in_.shape or in_next.dtype != in_.dtype or not in_next.is_contiguous():
+        raise PrkError(-1, "in_next must match in")
+    check(load().prk_gb300_stencil_steps(pattern, radius, n, dt, steps, in_.data_ptr(), in_next.data_ptr(),
+                                         out.data_ptr(), _stream(stream)))
+
+
 def _make_op(pattern: int, radius: int):
     def op(n: int, t: int, in_, out) -> None:
         if _n_of(in_) != n:
@@ -150,13 +162,13 @@ class RunResult:
 
 
 def run(pattern: int, radius: int, iterations: int, in_a, in_b, out, graph: bool = False, unfused: bool = False,
-        stream=None) -> RunResult:
+        stream=None, depth: int = 1) -> RunResult:
     n = _n_of(in_a)
     dt = dtype_of(in_a)
     _check_out(out, n, dt)
     el = C.c_double()
     fin = C.c_int()
-    flags = (RUN_GRAPH if graph else 0) | (RUN_UNFUSED if unfused else 0)
+    flags = (RUN_GRAPH if graph else 0) | (RUN_UNFUSED if unfused else 0) | (depth << 8)
     check(load().prk_gb300_run(pattern, radius, n, dt, iterations, in_a.data_ptr(),
                                None if in_b is None else in_b.data_ptr(), out.data_ptr(), flags, C.byref(el),
                                C.byref(fin), _stream(stream)))

@@ -24,6 +24,7 @@ _pi = C.POINTER(C.c_int)
 # name -> (restype, argtypes); kept in the order of include/prk_gb300.h
 SIGNATURES: dict[str, tuple] = {
     "prk_gb300_stencil": (_int, [_int, _int, _i64, _int, _vp, _vp, _vp, _vp]),
+    "prk_gb300_stencil_steps": (_int, [_int, _int, _i64, _int, _int, _vp, _vp, _vp, _vp]),
     "prk_gb300_add": (_int, [_i64, _int, _vp, _vp]),
     "prk_gb300_init": (_int, [_i64, _int, _vp, _vp, _vp]),
     "prk_gb300_norm": (_int, [_int, _i64, _int, _vp, _pd, _vp]),

@@ -20,9 +20,11 @@ PKG = Path(__file__).resolve().parent
 ROOT = PKG.parent
 CSRC = PKG / "csrc"
 HOST = PKG / "host"
-BUILD = PKG / "_build"
+BUILD = Path(os.environ.get("PRK_BUILD_DIR", PKG / "_build"))
 LIB = BUILD / "libprk_gb300.so"
 CLI = BUILD / "stencil-gb300"
+# extra nvcc options (e.g. -DPRK_TILE_STAGES=2) for a variant build in PRK_BUILD_DIR
+EXTRA = os.environ.get("PRK_NVCC_EXTRA", "").split()
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills",
@@ -63,7 +65,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     jobs = []
     for src, obj in zip(sources, objs):
         if force or _stale(obj, [src, *headers]):
-            jobs.append([nvcc, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)])
+            jobs.append([nvcc, *NVCC_FLAGS, *EXTRA, "-c", str(src), "-o", str(obj)])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             for f in [ex.submit(_run, j) for j in jobs]:

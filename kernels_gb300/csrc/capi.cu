@@ -114,10 +114,25 @@ int launch_one(int pattern, int radius, int64_t n, int dtype, const void* in, vo
     if (tma) {
         DevScratch d;
         if (int rc = dev_scratch(&d)) return rc;
-        PRK_CUDA(prk::launch_stencil_tma(c, d.status), "stencil launch (TMA tiles)");
+        PRK_CUDA(prk::launch_stencil_tma(c, 1, d.status), "stencil launch (TMA tiles)");
     } else {
         PRK_CUDA(prk::launch_stencil_generic(c), "stencil launch");
     }
+    return PRK_OK;
+}
+
+// `steps` fused applications from in into in_next in one launch (TMA tiles only).
+int launch_steps(int pattern, int radius, int64_t n, int dtype, int steps, const void* in, void* in_next, void* out,
+                 cudaStream_t s)
+{
+    prk::StencilCall c{pattern, radius, n, dtype, in, in_next, out, s};
+    if (!prk::tma_depth_ok(steps)) return fail(PRK_ERR_ARG, "temporal depth %d is not 1, 2, 4 or 8", steps);
+    if (!prk::tma_eligible(c) || g_kernel_choice == 1)
+        return fail(PRK_ERR_ARG, "temporal blocking needs the TMA tile kernels: 16-byte-aligned buffers, n a multiple of %d",
+                    dtype == PRK_FP64 ? 2 : 4);
+    DevScratch d;
+    if (int rc = dev_scratch(&d)) return rc;
+    PRK_CUDA(prk::launch_stencil_tma(c, steps, d.status), "stencil launch (TMA tiles, temporal)");
     return PRK_OK;
 }
 
@@ -181,6 +196,17 @@ int prk_gb300_stencil(int pattern, int radius, int64_t n, int dtype, const void*
     return launch_one(pattern, radius, n, dtype, in, in_next, out, static_cast<cudaStream_t>(stream));
 }
 
+int prk_gb300_stencil_steps(int pattern, int radius, int64_t n, int dtype, int steps, const void* in, void* in_next,
+                            void* out, void* stream)
+{
+    if (int rc = check_stencil(pattern, radius, n, dtype)) return rc;
+    if (!in || !in_next || !out) return fail(PRK_ERR_ARG, "in, in_next and out must be non-null device pointers");
+    const int64_t ib = prk_gb300_bytes(n, dtype, 0), ob = prk_gb300_bytes(n, dtype, 1);
+    if (overlaps(in, ib, out, ob) || overlaps(in_next, ib, in, ib) || overlaps(in_next, ib, out, ob))
+        return fail(PRK_ERR_ARG, "buffers overlap");
+    return launch_steps(pattern, radius, n, dtype, steps, in, in_next, out, static_cast<cudaStream_t>(stream));
+}
+
 int prk_gb300_add(int64_t n, int dtype, void* in, void* stream)
 {
     if (dtype != PRK_FP64 && dtype != PRK_FP32C) return fail(PRK_ERR_ARG, "dtype %d is not PRK_FP64 or PRK_FP32C", dtype);
@@ -217,6 +243,9 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
     if (iterations < 1) return fail(PRK_ERR_ARG, "iterations must be >= 1");
     const bool unfused = (flags & PRK_RUN_UNFUSED) != 0;
     const bool graph = (flags & PRK_RUN_GRAPH) != 0;
+    int depth = (flags >> 8) & 0xFF;
+    if (depth == 0) depth = 1;
+    if (!prk::tma_depth_ok(depth)) return fail(PRK_ERR_ARG, "temporal depth %d is not 1, 2, 4 or 8", depth);
     if (!in_a || !out || (!unfused && !in_b)) return fail(PRK_ERR_ARG, "null buffer");
     const int64_t ib = prk_gb300_bytes(n, dtype, 0), ob = prk_gb300_bytes(n, dtype, 1);
     if (overlaps(in_a, ib, out, ob) || (!unfused && (overlaps(in_b, ib, out, ob) || overlaps(in_a, ib, in_b, ib))))
@@ -231,6 +260,10 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
     }
     void* bufs[2] = {in_a, in_b};
     int cur = 0;
+    {
+        prk::StencilCall probe{pattern, radius, n, dtype, in_a, in_b, out, nullptr};
+        if (unfused || g_kernel_choice == 1 || !prk::tma_eligible(probe)) depth = 1;
+    }
     auto step = [&](cudaStream_t st) -> int {
         if (unfused) {
             if (int rc = launch_one(pattern, radius, n, dtype, in_a, nullptr, out, st)) return rc;
@@ -238,6 +271,22 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
         } else {
             if (int rc = launch_one(pattern, radius, n, dtype, bufs[cur], bufs[cur ^ 1], out, st)) return rc;
             cur ^= 1;
+        }
+        return PRK_OK;
+    };
+    // `count` applications: launches of the temporal depth, the remainder in powers of two.
+    auto steps = [&](cudaStream_t st, int count) -> int {
+        if (depth == 1) {
+            for (int i = 0; i < count; ++i)
+                if (int rc = step(st)) return rc;
+            return PRK_OK;
+        }
+        while (count > 0) {
+            int d = depth;
+            while (d > count) d >>= 1;
+            if (int rc = launch_steps(pattern, radius, n, dtype, d, bufs[cur], bufs[cur ^ 1], out, st)) return rc;
+            cur ^= 1;
+            count -= d;
         }
         return PRK_OK;
     };
@@ -259,7 +308,7 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
         if ((rc = step(s)) != PRK_OK) break;  // iteration 0: untimed warm-up
         if (graph) {
             if ((ce = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) { rc = cuda_fail(ce, "cudaStreamBeginCapture"); break; }
-            for (int it = 1; it <= iterations && rc == PRK_OK; ++it) rc = step(s);
+            rc = steps(s, iterations);
             cudaError_t ec = cudaStreamEndCapture(s, &g);
             if (rc != PRK_OK) break;
             if (ec != cudaSuccess) { rc = cuda_fail(ec, "cudaStreamEndCapture"); break; }
@@ -270,7 +319,7 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
             cudaEventRecord(e1, s);
         } else {
             cudaEventRecord(e0, s);
-            for (int it = 1; it <= iterations && rc == PRK_OK; ++it) rc = step(s);
+            rc = steps(s, iterations);
             if (rc != PRK_OK) break;
             cudaEventRecord(e1, s);
         }

@@ -27,10 +27,12 @@ constexpr int64_t NMAX = 65535LL * 16;
 inline int64_t in_elem_bytes(int dtype) { return dtype == FP64 ? 8 : 4; }
 inline int64_t out_elem_bytes(int dtype) { return 8; }
 
-// kernels_tma.cu: the TMA tile kernels, for the fused form on 16-byte-aligned buffers and rows.
-// `status` is a device word; bit 0 is set if a bounded wait gave up.
+// tile_host.cu: the TMA tile kernels, for the fused form on 16-byte-aligned buffers and rows.
+// `steps` consecutive applications per launch (temporal depth 1, 2, 4 or 8). `status` is a device
+// word; bit 0 is set if a bounded wait gave up.
 bool tma_eligible(const StencilCall& c);
-cudaError_t launch_stencil_tma(const StencilCall& c, unsigned* status);
+bool tma_depth_ok(int steps);
+cudaError_t launch_stencil_tma(const StencilCall& c, int steps, unsigned* status);
 
 // kernels_generic.cu: any n, any 8-byte-aligned pointers.
 cudaError_t launch_stencil_generic(const StencilCall& c);

@@ -1,0 +1,591 @@
+// The TMA tile kernel, templated on pattern, radius, storage form and temporal depth.
+//
+// One CTA per TH x TW tile of the grid, as many resident per SM as shared memory allows. The elected
+// thread issues two 2D TMA loads that complete on one mbarrier: the `in` tile with its halo and the
+// `out` tile. The halo is R rows above and below and RA >= R columns either side, RA rounded up to
+// 16 bytes so every TMA x coordinate is 16-byte aligned; the hardware zero-fills what lies outside
+// the grid. The resident CTAs of an SM overlap one another's loads and evaluation. (A persistent
+// variant with a ring of stages per CTA measured slower here: fewer warps per SM to evaluate each
+// tile, and CTAs drifting apart in the raster order.)
+//
+// In a tile, lane l owns CPT adjacent columns (one 16-byte vector) and warp w owns rows w, w+8,
+// w+16, w+24. in_next and out go straight to HBM with 16-byte stores.
+//
+// Temporal depth STEPS: the tile applies STEPS consecutive applications before writing back.
+// `in` evolves pointwise (in_{k+1} = in_k + 1, Cxx11/stencil-openmp.cc:208-218), so the copy in
+// shared memory, halo included, is advanced in place with the same rounded +1 the reference
+// applies, and the halo never grows. Every application reads the current `in` values and applies
+// every tap. `out` stays in registers and is rounded after each application as the reference
+// rounds it. HBM traffic per application drops by STEPS.
+//
+// Evaluation modes:
+//   FP64, strict   every point in the reference order with binary64 instructions (bit-exact)
+//   FP64, exact    power-of-two stencils on a certified tile: integer evaluation with identical
+//                  bits (prk_fixed.cuh), falling back to strict per tile
+//   FP32C          paired antisymmetric differences from register row segments, split weights,
+//                  TwoSum, two-float out (prk_arith.cuh)
+#pragma once
+
+#include <cuda.h>
+
+#include "prk_arith.cuh"
+#include "prk_fixed.cuh"
+#include "prk_internal.cuh"
+#include "prk_ptx.cuh"
+
+namespace prk {
+namespace tile {
+
+constexpr int THREADS = 256;
+constexpr int WARPS = THREADS / 32;
+
+template <int DT>
+struct Cfg;
+template <>
+struct Cfg<FP64> {
+    using T = double;
+    static constexpr int TW = 64, TH = 32, CPT = 2, VEC = 2;
+};
+template <>
+struct Cfg<FP32C> {
+    using T = float;
+    static constexpr int TW = 128, TH = 32, CPT = 4, VEC = 4;
+};
+
+constexpr int SMEM_PER_SM = 228 * 1024;
+constexpr int SMEM_PER_CTA_MAX = 227 * 1024;
+
+template <int DT, int R>
+struct Geo {
+    using C = Cfg<DT>;
+    using T = typename C::T;
+    static constexpr int RA = ((R + C::VEC - 1) / C::VEC) * C::VEC;  // halo columns, 16-byte multiple
+    static constexpr int SW = C::TW + 2 * RA;                        // in-tile row length = TMA box x
+    static constexpr int SH = C::TH + 2 * R;                         // in-tile rows = TMA box y
+    static constexpr int IN_BYTES = SW * SH * static_cast<int>(sizeof(T));
+    static constexpr int OUT_BYTES = C::TW * C::TH * 8;
+    static constexpr int OUT_OFF = (IN_BYTES + 127) / 128 * 128;     // out tile
+    static constexpr int RED_OFF = OUT_OFF + OUT_BYTES;              // per-warp words of the certification
+    static constexpr int BAR_OFF = RED_OFF + WARPS * 8;
+    static constexpr int SMEM = BAR_OFF + 8;
+    static constexpr int CTAS_FIT = SMEM_PER_SM / (SMEM + 1024);     // 1 KB per CTA is reserved
+    static constexpr int CTAS = CTAS_FIT > 8 ? 8 : CTAS_FIT;         // resident CTAs per SM
+    static constexpr int ELEMS = SW * SH;
+    static constexpr int ROWS = C::TH / WARPS;
+    static_assert(SMEM <= SMEM_PER_CTA_MAX && CTAS >= 1, "the tile must fit in shared memory");
+    static_assert(SW <= 256 && SH <= 256 && C::TW <= 256, "TMA box dimensions are at most 256");
+    static_assert((SW * sizeof(T)) % 16 == 0, "TMA box rows must be 16-byte multiples");
+    static_assert(C::TH % WARPS == 0 && C::TW == 32 * C::CPT, "thread layout");
+};
+
+// Everything a launch needs besides the template arguments.
+struct Launch {
+    CUtensorMap tm_in;
+    CUtensorMap tm_out;
+    int64_t n;
+    void* in_next;
+    void* out;
+    unsigned* status;
+    cudaStream_t stream;
+};
+
+// ---------------------------------------------------------------------------------------------
+// 16-byte vector access helpers
+
+__device__ __forceinline__ void st_vec(double* p, const double (&v)[2])
+{
+    *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+}
+__device__ __forceinline__ void st_vec(float* p, const float (&v)[4])
+{
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+
+// N consecutive floats from 16-byte-aligned shared memory.
+template <int N>
+__device__ __forceinline__ void ld_seg(const float* p, float (&v)[N])
+{
+    static_assert(N % 4 == 0, "segment is whole float4 vectors");
+#pragma unroll
+    for (int q = 0; q < N / 4; ++q) {
+        const float4 t = reinterpret_cast<const float4*>(p)[q];
+        v[4 * q] = t.x;
+        v[4 * q + 1] = t.y;
+        v[4 * q + 2] = t.z;
+        v[4 * q + 3] = t.w;
+    }
+}
+
+// N consecutive fixed-point words from 16-byte-aligned shared memory, narrowed to I.
+template <int N, typename I>
+__device__ __forceinline__ void ld_seg_i(const int64_t* p, I (&v)[N])
+{
+    static_assert(N % 2 == 0, "segment is whole 16-byte vectors");
+#pragma unroll
+    for (int q = 0; q < N / 2; ++q) {
+        const longlong2 t = reinterpret_cast<const longlong2*>(p)[q];
+        v[2 * q] = static_cast<I>(t.x);
+        v[2 * q + 1] = static_cast<I>(t.y);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// FP32C: the stencil sums of CPT points of one row. s points at in(r, c0) in the smem tile.
+
+template <int P, int R, int CPT, int RA>
+__device__ __forceinline__ void fp32c_points(const float* s, int ld, float (&sh)[CPT], float (&sl)[CPT])
+{
+    constexpr int SEG = CPT + 2 * RA;
+    bool first = true;
+    auto acc = [&](int k, float w_hi, float w_lo, float d) {
+        const float p = __fmul_rn(w_hi, d);
+        float pe = __fmaf_rn(w_hi, d, -p);
+        pe = __fmaf_rn(w_lo, d, pe);
+        if (first) {
+            sh[k] = p;
+            sl[k] = pe;
+        } else {
+            float t, e;
+            two_sum(sh[k], p, t, e);
+            sh[k] = t;
+            sl[k] = __fadd_rn(sl[k], __fadd_rn(e, pe));
+        }
+    };
+    {
+        float m0[SEG];
+        ld_seg<SEG>(s - RA, m0);
+#pragma unroll
+        for (int dc = 1; dc <= R; ++dc) {
+            const double w = weight(P, R, dc, 0);
+#pragma unroll
+            for (int k = 0; k < CPT; ++k) acc(k, split_hi(w), split_lo(w), __fsub_rn(m0[k + RA + dc], m0[k + RA - dc]));
+            first = false;
+        }
+    }
+#pragma unroll
+    for (int dr = 1; dr <= R; ++dr) {
+        if constexpr (P == STAR) {
+            float up[CPT], dn[CPT];
+            ld_seg<CPT>(s + dr * ld, up);
+            ld_seg<CPT>(s - dr * ld, dn);
+            const double w = weight(P, R, 0, dr);
+#pragma unroll
+            for (int k = 0; k < CPT; ++k) acc(k, split_hi(w), split_lo(w), __fsub_rn(up[k], dn[k]));
+        } else {
+            float up[SEG], dn[SEG];
+            ld_seg<SEG>(s + dr * ld - RA, up);
+            ld_seg<SEG>(s - dr * ld - RA, dn);
+#pragma unroll
+            for (int dc = -R; dc <= R; ++dc) {
+                const double w = weight(P, R, dc, dr);
+                if (w != 0.0) {
+#pragma unroll
+                    for (int k = 0; k < CPT; ++k)
+                        acc(k, split_hi(w), split_lo(w), __fsub_rn(up[k + RA + dc], dn[k + RA - dc]));
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// FP64 exact route: integer coefficients c = w * 2^shift of a power-of-two stencil.
+
+template <int P, int R>
+__device__ __forceinline__ constexpr int coef(int dc, int dr)
+{
+    const int d = weight_den(P, R, dc, dr);
+    return d == 0 ? 0 : weight_sign(P, R, dc, dr) * ((1 << pow2_shift(P, R)) / d);
+}
+
+// sum of c * (V[p+d] - V[p-d]) over the positive taps for CPT points of a row; v points at V(r, c0).
+template <int P, int R, int CPT, int RA, typename I>
+__device__ __forceinline__ void fx_points(const int64_t* v, int ld, I (&S)[CPT])
+{
+    constexpr int SEG = CPT + 2 * RA;
+#pragma unroll
+    for (int k = 0; k < CPT; ++k) S[k] = 0;
+    {
+        I m0[SEG];
+        ld_seg_i<SEG>(v - RA, m0);
+#pragma unroll
+        for (int dc = 1; dc <= R; ++dc) {
+            const int cc = coef<P, R>(dc, 0);
+#pragma unroll
+            for (int k = 0; k < CPT; ++k) S[k] += static_cast<I>(cc) * (m0[k + RA + dc] - m0[k + RA - dc]);
+        }
+    }
+#pragma unroll
+    for (int dr = 1; dr <= R; ++dr) {
+        if constexpr (P == STAR) {
+            I up[CPT], dn[CPT];
+            ld_seg_i<CPT>(v + dr * ld, up);
+            ld_seg_i<CPT>(v - dr * ld, dn);
+            const int cc = coef<P, R>(0, dr);
+#pragma unroll
+            for (int k = 0; k < CPT; ++k) S[k] += static_cast<I>(cc) * (up[k] - dn[k]);
+        } else {
+            I up[SEG], dn[SEG];
+            ld_seg_i<SEG>(v + dr * ld - RA, up);
+            ld_seg_i<SEG>(v - dr * ld - RA, dn);
+#pragma unroll
+            for (int dc = -R; dc <= R; ++dc) {
+                const int cc = coef<P, R>(dc, dr);
+                if (cc != 0) {
+#pragma unroll
+                    for (int k = 0; k < CPT; ++k) S[k] += static_cast<I>(cc) * (up[k + RA + dc] - dn[k + RA - dc]);
+                }
+            }
+        }
+    }
+}
+
+// binary64 encoding of x * 2^unit for a 32-bit x (exact).
+__device__ __forceinline__ uint64_t from_fixed32(int32_t x, int unit)
+{
+    if (x == 0) return 0;
+    const uint64_t s = x < 0 ? fx::SIGN : 0;
+    const uint32_t a = x < 0 ? static_cast<uint32_t>(-x) : static_cast<uint32_t>(x);
+    const int msb = 31 - __clz(a);
+    const uint64_t m = static_cast<uint64_t>(a) << (52 - msb);
+    return s | ((static_cast<uint64_t>(msb + unit + 1022) << 52) + m);
+}
+
+__device__ __forceinline__ uint64_t from_fixed_any(int64_t x, int unit) { return fx::from_fixed(x, unit); }
+__device__ __forceinline__ uint64_t from_fixed_any(int32_t x, int unit) { return from_fixed32(x, unit); }
+
+__device__ __forceinline__ double as_dbl(uint64_t b) { return __longlong_as_double(static_cast<long long>(b)); }
+__device__ __forceinline__ uint64_t as_bits(double d) { return static_cast<uint64_t>(__double_as_longlong(d)); }
+
+// ---------------------------------------------------------------------------------------------
+// The kernel
+
+// True when the tile at (i0, j0) holds interior points, i.e. has an out tile to load and update.
+__device__ __forceinline__ bool tile_has_out(int64_t i0, int64_t j0, int64_t n, int R, int tw, int th)
+{
+    return (i0 + th > R) && (i0 < n - R) && (j0 + tw > R) && (j0 < n - R);
+}
+
+// Evaluate one tile held in a stage: STEPS applications, then in_next and out to HBM.
+template <int P, int R, int DT, int STEPS>
+__device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, int64_t i0, int64_t j0, int64_t n,
+                                             bool has_out, void* __restrict__ in_next_v, void* __restrict__ out_v)
+{
+    using G = Geo<DT, R>;
+    using C = Cfg<DT>;
+    using T = typename C::T;
+    constexpr int CPT = C::CPT;
+    constexpr int ROWS = G::ROWS;
+    constexpr bool EXACT = DT == FP64 && pow2_weights(P, R);
+    T* s_in = reinterpret_cast<T*>(stage);
+    uint64_t* o_tile = reinterpret_cast<uint64_t*>(stage + G::OUT_OFF);
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c0 = lane * CPT;
+    const int64_t gj = j0 + c0;
+    const bool col_ok = gj < n;  // n % CPT == 0: a vector is wholly inside or outside the grid
+    const bool cols_interior = gj >= R && gj + CPT <= n - R;
+
+    // ---- FP64 power-of-two stencils: certify the tile for the exact integer route ----
+    int unit = fx::NOT_FIXED;
+    bool narrow = false;
+    if constexpr (EXACT) {
+        constexpr int SHIFT = pow2_shift(P, R);
+        constexpr long long L1 = pow2_coef_l1(P, R);
+        constexpr int PER = (G::ELEMS + THREADS - 1) / THREADS;
+        uint64_t vals[PER];
+        int lo = fx::ZERO_LO, hi = fx::ZERO_HI;
+        const uint64_t* raw = reinterpret_cast<const uint64_t*>(s_in);
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int idx = threadIdx.x + q * THREADS;
+            vals[q] = idx < G::ELEMS ? raw[idx] : 0ull;
+            int l, h;
+            fx::classify(vals[q], l, h);
+            lo = min(lo, l);
+            hi = max(hi, h);
+        }
+        lo = __reduce_min_sync(0xffffffffu, lo);
+        hi = __reduce_max_sync(0xffffffffu, hi);
+        if (lane == 0) {
+            s_red[2 * warp] = lo;
+            s_red[2 * warp + 1] = hi;
+        }
+        __syncthreads();
+        lo = s_red[0];
+        hi = s_red[1];
+#pragma unroll
+        for (int w = 1; w < WARPS; ++w) {
+            lo = min(lo, s_red[2 * w]);
+            hi = max(hi, s_red[2 * w + 1]);
+        }
+        unit = fx::certify(lo, hi, SHIFT, L1, STEPS);
+        if (unit != fx::NOT_FIXED) {
+            // int32 arithmetic suffices when every partial sum and every updated value stays below 2^31
+            const int span = hi == fx::ZERO_HI ? 0 : hi + 1 - unit;
+            narrow = span <= 30 && -unit <= 26 &&
+                     ((1ll << span) + static_cast<long long>(STEPS) * (1ll << (-unit))) < (1ll << 31) / L1;
+            int64_t* iv = reinterpret_cast<int64_t*>(s_in);
+#pragma unroll
+            for (int q = 0; q < PER; ++q) {
+                const int idx = threadIdx.x + q * THREADS;
+                if (idx < G::ELEMS) iv[idx] = fx::to_fixed(vals[q], unit);
+            }
+        }
+        __syncthreads();  // every converted word visible
+    }
+
+    // S of CPT points of row r (tile coordinates) added into the out words o[] (in place)
+    auto apply_row = [&](int r, uint64_t* o) {
+        const int soff = (r + R) * G::SW + G::RA + c0;  // in(r, c0) in the tile
+        if constexpr (DT == FP64) {
+            bool done = false;
+            if constexpr (EXACT) {
+                constexpr int SHIFT = pow2_shift(P, R);
+                const int64_t* v = reinterpret_cast<const int64_t*>(s_in) + soff;
+                if (unit != fx::NOT_FIXED) {
+                    if (narrow) {
+                        int32_t S[CPT];
+                        fx_points<P, R, CPT, G::RA>(v, G::SW, S);
+#pragma unroll
+                        for (int k = 0; k < CPT; ++k)
+                            o[k] = as_bits(__dadd_rn(as_dbl(o[k]), as_dbl(from_fixed32(S[k], unit - SHIFT))));
+                    } else {
+                        int64_t S[CPT];
+                        fx_points<P, R, CPT, G::RA>(v, G::SW, S);
+#pragma unroll
+                        for (int k = 0; k < CPT; ++k)
+                            o[k] = as_bits(__dadd_rn(as_dbl(o[k]), as_dbl(fx::from_fixed(S[k], unit - SHIFT))));
+                    }
+                    done = true;
+                }
+            }
+            if (!done) {
+                const double* sp = reinterpret_cast<const double*>(s_in) + soff;
+#pragma unroll
+                for (int k = 0; k < CPT; ++k) o[k] = as_bits(__dadd_rn(as_dbl(o[k]), fp64_point<P, R>(sp + k, G::SW)));
+            }
+        } else {
+            const float* sp = reinterpret_cast<const float*>(s_in) + soff;
+            float sh[CPT], sl[CPT];
+            fp32c_points<P, R, CPT, G::RA>(sp, G::SW, sh, sl);
+#pragma unroll
+            for (int k = 0; k < CPT; ++k) {
+                float oh = __uint_as_float(static_cast<uint32_t>(o[k]));
+                float ol = __uint_as_float(static_cast<uint32_t>(o[k] >> 32));
+                df_add(oh, ol, sh[k], sl[k]);
+                o[k] = static_cast<uint64_t>(__float_as_uint(oh)) | (static_cast<uint64_t>(__float_as_uint(ol)) << 32);
+            }
+        }
+    };
+
+    // in_next (in + 1 after the last application) and out of row r to HBM
+    auto store_row = [&](int r, const uint64_t* o, bool row_out) {
+        const int64_t gi = i0 + r;
+        const int soff = (r + R) * G::SW + G::RA + c0;
+        T nxt[CPT];
+        bool done = false;
+        if constexpr (EXACT) {
+            if (unit != fx::NOT_FIXED) {
+                const int64_t* v = reinterpret_cast<const int64_t*>(s_in) + soff;
+                const int64_t one = 1ll << (-unit);
+                if (narrow) {
+#pragma unroll
+                    for (int k = 0; k < CPT; ++k) nxt[k] = as_dbl(from_fixed32(static_cast<int32_t>(v[k] + one), unit));
+                } else {
+#pragma unroll
+                    for (int k = 0; k < CPT; ++k) nxt[k] = as_dbl(fx::from_fixed(v[k] + one, unit));
+                }
+                done = true;
+            }
+        }
+        if (!done) {
+#pragma unroll
+            for (int k = 0; k < CPT; ++k) {
+                if constexpr (DT == FP64)
+                    nxt[k] = __dadd_rn(s_in[soff + k], 1.0);
+                else
+                    nxt[k] = __fadd_rn(s_in[soff + k], 1.0f);
+            }
+        }
+        st_vec(static_cast<T*>(in_next_v) + gi * n + gj, nxt);
+        if (row_out) {
+            uint64_t* out = static_cast<uint64_t*>(out_v) + gi * n + gj;
+            if (cols_interior) {
+#pragma unroll
+                for (int k = 0; k < CPT; k += 2) *reinterpret_cast<ulonglong2*>(out + k) = make_ulonglong2(o[k], o[k + 1]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < CPT; ++k)
+                    if (gj + k >= R && gj + k < n - R) out[k] = o[k];
+            }
+        }
+    };
+
+    if constexpr (STEPS == 1) {
+        // one pass: each row's new out and in_next leave as soon as they are computed
+#pragma unroll
+        for (int rr = 0; rr < ROWS; ++rr) {
+            const int r = warp + WARPS * rr;
+            const int64_t gi = i0 + r;
+            if (!col_ok || gi >= n) continue;
+            const bool row_out = has_out && gi >= R && gi < n - R;
+            uint64_t o[CPT];
+            if (row_out) {
+#pragma unroll
+                for (int k = 0; k < CPT; ++k) o[k] = o_tile[r * C::TW + c0 + k];
+                apply_row(r, o);
+            }
+            store_row(r, o, row_out);
+        }
+    } else {
+        // out of the thread's points stays in registers across the applications
+        uint64_t o[ROWS][CPT];
+#pragma unroll
+        for (int rr = 0; rr < ROWS; ++rr) {
+            const int r = warp + WARPS * rr;
+            const int64_t gi = i0 + r;
+            const bool row_out = col_ok && gi < n && has_out && gi >= R && gi < n - R;
+#pragma unroll
+            for (int k = 0; k < CPT; ++k) o[rr][k] = row_out ? o_tile[r * C::TW + c0 + k] : 0ull;
+        }
+#pragma unroll 1
+        for (int t = 0; t < STEPS; ++t) {
+            if (t > 0) {  // advance the whole tile, halo included: in_{k+1} = in_k + 1
+                __syncthreads();
+                for (int idx = threadIdx.x; idx < G::ELEMS; idx += THREADS) {
+                    if constexpr (DT == FP64) {
+                        if (EXACT && unit != fx::NOT_FIXED)
+                            reinterpret_cast<int64_t*>(s_in)[idx] += (1ll << (-unit));
+                        else
+                            s_in[idx] = __dadd_rn(s_in[idx], 1.0);
+                    } else {
+                        s_in[idx] = __fadd_rn(s_in[idx], 1.0f);
+                    }
+                }
+                __syncthreads();
+            }
+#pragma unroll
+            for (int rr = 0; rr < ROWS; ++rr) {
+                const int r = warp + WARPS * rr;
+                const int64_t gi = i0 + r;
+                if (!col_ok || gi >= n || !(has_out && gi >= R && gi < n - R)) continue;
+                apply_row(r, o[rr]);
+            }
+        }
+#pragma unroll
+        for (int rr = 0; rr < ROWS; ++rr) {
+            const int r = warp + WARPS * rr;
+            const int64_t gi = i0 + r;
+            if (!col_ok || gi >= n) continue;
+            store_row(r, o[rr], has_out && gi >= R && gi < n - R);
+        }
+    }
+}
+
+// Register budget: the single-application kernels keep as many tiles resident as shared memory
+// allows, so that every SM has enough loads in flight; the multi-application kernels hold `out` in
+// registers and run at most four tiles per SM. The strict FP64 form is bound by the binary64 pipe
+// and gets the registers its unrolled tap sequence wants.
+template <int P, int R, int DT, int STEPS>
+constexpr int min_blocks()
+{
+    if (DT == FP64 && !pow2_weights(P, R)) return STEPS == 1 ? 2 : 1;
+    const int b = Geo<DT, R>::CTAS;
+    return STEPS == 1 ? b : (b < 3 ? b : 3);
+}
+
+// One CTA per tile: blockIdx = (tile column, tile row). The elected thread issues the tile's two TMA
+// loads; every thread waits on the mbarrier with a bounded spin, and on a timeout the CTA flags
+// `status`, waits (again bounded) for the copies to land and returns.
+template <int P, int R, int DT, int STEPS>
+__global__ void __launch_bounds__(THREADS, min_blocks<P, R, DT, STEPS>())
+    k_stencil_tile(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ CUtensorMap tm_out,
+                   const int64_t n, void* __restrict__ in_next_v, void* __restrict__ out_v, unsigned* __restrict__ status)
+{
+    using G = Geo<DT, R>;
+    using C = Cfg<DT>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    int* s_red = reinterpret_cast<int*>(smem + G::RED_OFF);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + G::BAR_OFF);
+    const int64_t i0 = static_cast<int64_t>(blockIdx.y) * C::TH;
+    const int64_t j0 = static_cast<int64_t>(blockIdx.x) * C::TW;
+    const bool has_out = tile_has_out(i0, j0, n, R, C::TW, C::TH);
+
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+        mbar_arrive_expect_tx(bar, G::IN_BYTES + (has_out ? G::OUT_BYTES : 0));
+        tma_load_2d(smem, &tm_in, static_cast<int32_t>(j0 - G::RA), static_cast<int32_t>(i0 - R), bar);
+        if (has_out) tma_load_2d(smem + G::OUT_OFF, &tm_out, static_cast<int32_t>(j0), static_cast<int32_t>(i0), bar);
+    }
+    __syncthreads();
+    if (!mbar_wait_bounded(bar, 0)) {
+        if (threadIdx.x == 0) atomicOr(status, 1u);
+        mbar_wait_bounded(bar, 0);  // let the copies land before the CTA's shared memory is released
+        return;
+    }
+    process_tile<P, R, DT, STEPS>(smem, s_red, i0, j0, n, has_out, in_next_v, out_v);
+}
+
+template <int P, int R, int DT, int STEPS>
+cudaError_t launch(const Launch& L)
+{
+    using G = Geo<DT, R>;
+    using C = Cfg<DT>;
+    if (cudaError_t e = cudaFuncSetAttribute(k_stencil_tile<P, R, DT, STEPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM))
+        return e;
+    const int64_t tx = (L.n + C::TW - 1) / C::TW, ty = (L.n + C::TH - 1) / C::TH;
+    if (ty > 65535) return cudaErrorInvalidValue;
+    const dim3 grid(static_cast<unsigned>(tx), static_cast<unsigned>(ty));
+    k_stencil_tile<P, R, DT, STEPS><<<grid, THREADS, G::SMEM, L.stream>>>(L.tm_in, L.tm_out, L.n, L.in_next, L.out, L.status);
+    return cudaGetLastError();
+}
+
+// Supported temporal depths; a run of any length is split into launches of these.
+constexpr int MAX_STEPS = 8;
+
+template <int P, int DT>
+cudaError_t launch_pattern(int R, int steps, const Launch& L)
+{
+#define PRK_TILE_CASE(RR)                                        \
+    case RR:                                                     \
+        switch (steps) {                                         \
+        case 1: return launch<P, RR, DT, 1>(L);                  \
+        case 2: return launch<P, RR, DT, 2>(L);                  \
+        case 4: return launch<P, RR, DT, 4>(L);                  \
+        case 8: return launch<P, RR, DT, 8>(L);                  \
+        default: return cudaErrorInvalidValue;                   \
+        }
+    switch (R) {
+        PRK_TILE_CASE(1)
+        PRK_TILE_CASE(2)
+        PRK_TILE_CASE(3)
+        PRK_TILE_CASE(4)
+        PRK_TILE_CASE(5)
+    }
+#undef PRK_TILE_CASE
+    return cudaErrorInvalidValue;
+}
+
+// Tile geometry for the host: box sizes of the two tensor maps.
+inline void boxes(int dtype, int R, int* in_x, int* in_y, int* out_x, int* out_y)
+{
+    const int vec = dtype == FP64 ? 2 : 4;
+    const int ra = ((R + vec - 1) / vec) * vec;
+    const int tw = dtype == FP64 ? Cfg<FP64>::TW : Cfg<FP32C>::TW;
+    const int th = dtype == FP64 ? Cfg<FP64>::TH : Cfg<FP32C>::TH;
+    *in_x = tw + 2 * ra;
+    *in_y = th + 2 * R;
+    *out_x = tw;
+    *out_y = th;
+}
+
+// Per-translation-unit entry points (tile_*.cu).
+cudaError_t launch_fp64_star(int R, int steps, const Launch& L);
+cudaError_t launch_fp64_grid(int R, int steps, const Launch& L);
+cudaError_t launch_fp32c_star(int R, int steps, const Launch& L);
+cudaError_t launch_fp32c_grid(int R, int steps, const Launch& L);
+
+}  // namespace tile
+}  // namespace prk

@@ -1,0 +1,75 @@
+// Host side of the TMA tile kernels: eligibility, tensor-map encoding and dispatch to the
+// per-form instantiations (tile_*.cu). cuTensorMapEncodeTiled is fetched from the driver at run
+// time, so the library does not link libcuda.
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
+#include "stencil_tile.cuh"
+
+namespace prk {
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::once_flag g_encode_once;
+cudaError_t g_encode_err = cudaSuccess;
+
+cudaError_t encoder(PFN_cuTensorMapEncodeTiled_v12000* fn)
+{
+    std::call_once(g_encode_once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        g_encode_err = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
+        if (g_encode_err == cudaSuccess && q != cudaDriverEntryPointSuccess) g_encode_err = cudaErrorNotSupported;
+        g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    *fn = g_encode;
+    return g_encode_err;
+}
+
+// A 2D map over an n x n row-major array of elem_bytes elements, box (box_x, box_y), zero fill.
+cudaError_t make_map(CUtensorMap* map, const void* base, int64_t n, int elem_bytes, int box_x, int box_y)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 enc = nullptr;
+    if (cudaError_t e = encoder(&enc)) return e;
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(n), static_cast<cuuint64_t>(n)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(n) * elem_bytes};
+    const cuuint32_t box[2] = {static_cast<cuuint32_t>(box_x), static_cast<cuuint32_t>(box_y)};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUtensorMapDataType dt = elem_bytes == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    const CUresult r = enc(map, dt, 2, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+bool tma_eligible(const StencilCall& c)
+{
+    if (!c.in_next) return false;  // the reference-operator form (no in_next) uses the generic kernel
+    const int vec = c.dtype == FP64 ? 2 : 4;
+    auto al16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
+    return c.n % vec == 0 && c.n >= 8 && al16(c.in) && al16(c.in_next) && al16(c.out);
+}
+
+bool tma_depth_ok(int steps) { return steps == 1 || steps == 2 || steps == 4 || steps == 8; }
+
+cudaError_t launch_stencil_tma(const StencilCall& c, int steps, unsigned* status)
+{
+    if (!tma_depth_ok(steps)) return cudaErrorInvalidValue;
+    tile::Launch L{};
+    int ix, iy, ox, oy;
+    tile::boxes(c.dtype, c.R, &ix, &iy, &ox, &oy);
+    if (cudaError_t e = make_map(&L.tm_in, c.in, c.n, c.dtype == FP64 ? 8 : 4, ix, iy)) return e;
+    if (cudaError_t e = make_map(&L.tm_out, c.out, c.n, 8, ox, oy)) return e;
+    L.n = c.n;
+    L.in_next = c.in_next;
+    L.out = c.out;
+    L.status = status;
+    L.stream = c.stream;
+    if (c.dtype == FP64) return c.pattern == STAR ? tile::launch_fp64_star(c.R, steps, L) : tile::launch_fp64_grid(c.R, steps, L);
+    return c.pattern == STAR ? tile::launch_fp32c_star(c.R, steps, L) : tile::launch_fp32c_grid(c.R, steps, L);
+}
+
+}  // namespace prk
