@@ -135,6 +135,72 @@ int prk_gb300_config(int key, int value);
  * prk_gb300_run checks it after every run. */
 int prk_gb300_status(void);
 
+/* ---- Autotuner ----------------------------------------------------------------------------
+ * Picks, per (pattern, radius, n, dtype), the kernel family, tile shape, thread coarsening and
+ * temporal depth by timing the candidates on scratch buffers of the same shape (n capped at 8192;
+ * larger grids share the 8192 result, their per-point cost being the same). Results are kept in
+ * memory and in a cache file, one JSON object per line: $PRK_GB300_TUNE_CACHE, else
+ * $HOME/.cache/prk_gb300/tune.jsonl. No counterpart in the reference (whose tile size is a CLI
+ * argument, Cxx11/stencil-openmp.cc:111-116). */
+typedef struct {
+    int depth;                      /* applications per launch: 1, 2, 4 or 8 */
+    int kernel;                     /* 1 = generic kernels, 2 = TMA tile kernels, 3 = batched kernel */
+    int tile_rows;                  /* tile shape (rows x columns) of the chosen kernel */
+    int tile_cols;
+    int cols_per_thread;            /* thread coarsening: adjacent columns each thread owns */
+    double seconds_per_application; /* measured on the scratch grid */
+    int from_cache;                 /* 1 when the result came from the cache */
+} prk_gb300_tuning;
+
+#define PRK_TUNE_BATCH 1 /* tune the batched kernel for a grid of this n */
+#define PRK_TUNE_FORCE 2 /* measure again even when cached */
+int prk_gb300_tune(int pattern, int radius, int64_t n, int dtype, int flags, prk_gb300_tuning* result);
+
+/* Flag for prk_gb300_run: take the temporal depth and kernel family from prk_gb300_tune. */
+#define PRK_RUN_TUNED 4
+
+/* ---- Batched grids ------------------------------------------------------------------------
+ * Many independent PRK grids of uneven n, mixed radius and pattern, advanced together: every launch
+ * is one persistent kernel over the tiles of all grids, which CTAs take from a device work queue.
+ * No counterpart in the reference, where each grid is a separate run of the driver
+ * (Cxx11/stencil-openmp.cc). One grid's buffers follow the prk_gb300_run conventions: in_a holds
+ * the initial in, in_b the second in buffer, out the accumulator; any n >= 2R+1 and alignment. */
+typedef struct {
+    int pattern;
+    int radius;
+    int64_t n;
+    void* in_a;
+    void* in_b;
+    void* out;
+} prk_gb300_grid;
+
+typedef struct prk_gb300_batch prk_gb300_batch;
+
+/* Builds a batch over `count` grids of one dtype (the descriptors are copied; the buffers stay
+ * caller-owned). flags: PRK_RUN_DEPTH(d) fixes the temporal depth of every grid; PRK_BATCH_TUNED
+ * takes each grid's depth from the autotuner (prk_gb300_tune), grouping grids by depth. Allocates
+ * the batch's device tables. */
+#define PRK_BATCH_TUNED 0x10000
+int prk_gb300_batch_create(const prk_gb300_grid* grids, int count, int dtype, int flags, prk_gb300_batch** batch);
+
+/* iterations+1 fused applications of every grid of the batch (application 0 untimed, as in
+ * prk_gb300_run). *elapsed_s gets the event time of applications 1..K. With PRK_RUN_GRAPH the
+ * timed launches are captured once into a CUDA graph (per iteration count) and replayed.
+ * Synchronous. */
+int prk_gb300_batch_run(prk_gb300_batch* batch, int iterations, int flags, double* elapsed_s, void* stream);
+
+/* 0 or 1: which of grid `index`'s buffers (in_a, in_b) holds its final in after the last run;
+ * negative for a bad index. */
+int prk_gb300_batch_final_in(const prk_gb300_batch* batch, int index);
+
+/* The interior L1 norm / (n-2R)^2 of every grid's out, into norms[count]. Synchronous. */
+int prk_gb300_batch_norms(prk_gb300_batch* batch, double* norms, void* stream);
+
+/* Launches per run of `iterations` (after the warm-up launch), for the benchmark's launch count. */
+int prk_gb300_batch_launches(const prk_gb300_batch* batch, int iterations);
+
+int prk_gb300_batch_destroy(prk_gb300_batch* batch);
+
 /* Bytes one buffer of the given role needs: role 0 = in / in_next, role 1 = out. */
 int64_t prk_gb300_bytes(int64_t n, int dtype, int role);
 

@@ -29,10 +29,10 @@ from ._lib import PrkError, check, load
 
 STAR, GRID = 0, 1
 FP64, FP32C = 0, 1
-RUN_GRAPH, RUN_UNFUSED = 1, 2
+RUN_GRAPH, RUN_UNFUSED, RUN_TUNED = 1, 2, 4
 
 __all__ = ["STAR", "GRID", "FP64", "FP32C", "PrkError", "apply", "add", "init", "norm", "run", "run_host",
-           "alloc", "apply_steps", "flops", "pattern_of", "dtype_of", "version", "set_kernel", "status", "KERNEL_AUTO",
+           "alloc", "apply_steps", "flops", "tune", "Batch", "pattern_of", "dtype_of", "version", "set_kernel", "status", "KERNEL_AUTO",
            "KERNEL_GENERIC", "KERNEL_TMA"] + \
           [f"{p}{r}" for p in ("star", "grid") for r in range(1, 6)]
 
@@ -162,13 +162,13 @@ class RunResult:
 
 
 def run(pattern: int, radius: int, iterations: int, in_a, in_b, out, graph: bool = False, unfused: bool = False,
-        stream=None, depth: int = 1) -> RunResult:
+        stream=None, depth: int = 1, tuned: bool = False) -> RunResult:
     n = _n_of(in_a)
     dt = dtype_of(in_a)
     _check_out(out, n, dt)
     el = C.c_double()
     fin = C.c_int()
-    flags = (RUN_GRAPH if graph else 0) | (RUN_UNFUSED if unfused else 0) | (depth << 8)
+    flags = (RUN_GRAPH if graph else 0) | (RUN_UNFUSED if unfused else 0) | (depth << 8) | (RUN_TUNED if tuned else 0)
     check(load().prk_gb300_run(pattern, radius, n, dt, iterations, in_a.data_ptr(),
                                None if in_b is None else in_b.data_ptr(), out.data_ptr(), flags, C.byref(el),
                                C.byref(fin), _stream(stream)))
@@ -187,6 +187,72 @@ def run_host(pattern: int, radius: int, iterations: int, h_in, h_out, h_in_final
                                     None if h_in_final is None else ptr(h_in_final), C.byref(nrm), C.byref(el),
                                     C.byref(ks)))
     return {"norm": nrm.value, "elapsed_s": el.value, "kernel_s": ks.value}
+
+
+def tune(pattern: int, radius: int, n: int, dtype: int = FP64, batch: bool = False, force: bool = False) -> dict:
+    """The autotuner's choice for (pattern, radius, n, dtype): kernel family, tile shape, thread
+    coarsening and temporal depth, measured on scratch buffers and cached (prk_gb300_tune)."""
+    from ._lib import Tuning
+    t = Tuning()
+    check(load().prk_gb300_tune(pattern, radius, n, dtype, (1 if batch else 0) | (2 if force else 0), C.byref(t)))
+    return {"depth": t.depth, "kernel": {1: "generic", 2: "tma", 3: "batched"}.get(t.kernel, str(t.kernel)),
+            "tile_rows": t.tile_rows, "tile_cols": t.tile_cols, "cols_per_thread": t.cols_per_thread,
+            "seconds_per_application": t.seconds_per_application, "from_cache": bool(t.from_cache)}
+
+
+class Batch:
+    """Many independent grids advanced together by the batched persistent kernel
+    (prk_gb300_batch_*). `grids` is a list of (pattern, radius, in_a, in_b, out) with device tensors;
+    all of one dtype. depth fixes the temporal depth; tuned=True takes it per grid from the tuner."""
+
+    def __init__(self, grids, depth: int | None = None, tuned: bool = False):
+        from ._lib import Grid
+        if not grids:
+            raise PrkError(-1, "a batch needs at least one grid")
+        self._tensors = grids  # keep the buffers alive
+        dt = dtype_of(grids[0][2])
+        arr = (Grid * len(grids))()
+        for k, (pattern, radius, in_a, in_b, out) in enumerate(grids):
+            n = _n_of(in_a)
+            if dtype_of(in_a) != dt:
+                raise PrkError(-1, "all grids of a batch share one dtype")
+            _check_out(out, n, dt)
+            arr[k] = Grid(pattern, radius, n, in_a.data_ptr(), in_b.data_ptr(), out.data_ptr())
+        flags = (depth or 0) << 8 | (0x10000 if tuned else 0)
+        h = C.c_void_p()
+        check(load().prk_gb300_batch_create(arr, len(grids), dt, flags, C.byref(h)))
+        self._h = h
+        self.dtype = dt
+
+    def run(self, iterations: int, graph: bool = False, stream=None) -> float:
+        el = C.c_double()
+        check(load().prk_gb300_batch_run(self._h, iterations, RUN_GRAPH if graph else 0, C.byref(el), _stream(stream)))
+        return el.value
+
+    def final_in(self, k: int):
+        which = load().prk_gb300_batch_final_in(self._h, k)
+        if which < 0:
+            raise PrkError(which, f"bad grid index {k}")
+        return self._tensors[k][2] if which == 0 else self._tensors[k][3]
+
+    def norms(self) -> list[float]:
+        out = (C.c_double * len(self._tensors))()
+        check(load().prk_gb300_batch_norms(self._h, out, _stream(None)))
+        return list(out)
+
+    def launches(self, iterations: int) -> int:
+        return int(load().prk_gb300_batch_launches(self._h, iterations))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            load().prk_gb300_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def alloc(n: int, dtype: int = FP64, device="cuda", ping_pong: bool = True):

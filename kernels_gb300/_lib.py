@@ -33,11 +33,30 @@ SIGNATURES: dict[str, tuple] = {
     "prk_gb300_run_host": (_int, [_int, _int, _i64, _int, _int, _vp, _vp, _vp, _pd, _pd, _pd]),
     "prk_gb300_config": (_int, [_int, _int]),
     "prk_gb300_status": (_int, []),
+    "prk_gb300_tune": (_int, [_int, _int, _i64, _int, _int, C.c_void_p]),
+    "prk_gb300_batch_create": (_int, [C.c_void_p, _int, _int, _int, C.c_void_p]),
+    "prk_gb300_batch_run": (_int, [_vp, _int, _int, _pd, _vp]),
+    "prk_gb300_batch_final_in": (_int, [_vp, _int]),
+    "prk_gb300_batch_norms": (_int, [_vp, _vp, _vp]),
+    "prk_gb300_batch_launches": (_int, [_vp, _int]),
+    "prk_gb300_batch_destroy": (_int, [_vp]),
     "prk_gb300_bytes": (_i64, [_i64, _int, _int]),
     "prk_gb300_flops": (_dbl, [_int, _int, _i64]),
     "prk_gb300_last_error": (C.c_char_p, []),
     "prk_gb300_version": (C.c_char_p, []),
 }
+
+class Tuning(C.Structure):
+    """prk_gb300_tuning (include/prk_gb300.h)."""
+    _fields_ = [("depth", C.c_int), ("kernel", C.c_int), ("tile_rows", C.c_int), ("tile_cols", C.c_int),
+                ("cols_per_thread", C.c_int), ("seconds_per_application", C.c_double), ("from_cache", C.c_int)]
+
+
+class Grid(C.Structure):
+    """prk_gb300_grid (include/prk_gb300.h)."""
+    _fields_ = [("pattern", C.c_int), ("radius", C.c_int), ("n", C.c_int64), ("in_a", C.c_void_p),
+                ("in_b", C.c_void_p), ("out", C.c_void_p)]
+
 
 _lib: C.CDLL | None = None
 

@@ -1,0 +1,23 @@
+// Instantiations of the batched kernel for fp32c storage, temporal depths 1, 2, 4, 8.
+#include "batch_kernel.cuh"
+
+namespace prk {
+namespace batch {
+
+cudaError_t launch_fp32c(int steps, const Launch& L) { return launch_depth<FP32C>(steps, L); }
+
+int ctas_per_sm_fp32c(int steps)
+{
+    int b = 0;
+    cudaError_t e = cudaErrorInvalidValue;
+    switch (steps) {
+    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<FP32C, 1>, tile::THREADS, Layout<FP32C>::SMEM); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<FP32C, 2>, tile::THREADS, Layout<FP32C>::SMEM); break;
+    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<FP32C, 4>, tile::THREADS, Layout<FP32C>::SMEM); break;
+    case 8: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<FP32C, 8>, tile::THREADS, Layout<FP32C>::SMEM); break;
+    }
+    return e == cudaSuccess ? b : 0;
+}
+
+}  // namespace batch
+}  // namespace prk

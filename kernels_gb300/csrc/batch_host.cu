@@ -1,0 +1,319 @@
+// Host side of the batched grids (prk_gb300_batch_*): device tables, the work-queue slots, the
+// launch sequence of a run and its CUDA graph.
+#include <algorithm>
+#include <cstdio>
+#include <map>
+#include <memory>
+#include <vector>
+
+#include "../../include/prk_gb300.h"
+#include "batch_kernel.cuh"
+#include "prk_internal.cuh"
+
+namespace {
+
+using prk::batch::GridDesc;
+
+int err(int code, const char* msg) { return prk::record_error(code, msg); }
+
+int cuda_err(cudaError_t e, const char* what)
+{
+    char msg[256];
+    std::snprintf(msg, sizeof msg, "%s: %s", what, cudaGetErrorString(e));
+    return prk::record_error(static_cast<int>(e), msg);
+}
+
+// Grids advanced by one kernel sequence: all of one temporal depth.
+struct Group {
+    int depth = 1;
+    std::vector<int> members;          // indices into the batch's grid list
+    GridDesc* d_desc = nullptr;        // device descriptors
+    int64_t* d_off = nullptr;          // device tile offsets (members + 1)
+    int64_t total = 0;                 // tiles over all members
+};
+
+}  // namespace
+
+struct prk_gb300_batch {
+    int dtype = PRK_FP64;
+    std::vector<prk_gb300_grid> grids;
+    std::vector<int> final_in;         // per grid, after the last run
+    std::vector<Group> groups;
+    GridDesc* d_all = nullptr;         // all grids, for the depth-1 warm-up launch
+    int64_t* d_all_off = nullptr;
+    int64_t all_total = 0;
+    unsigned long long* d_queue = nullptr;  // one work counter per launch of a run
+    int queue_slots = 0;
+    int ctas = 0;                      // persistent CTAs per launch
+    std::map<int, cudaGraphExec_t> graphs;  // per iteration count
+    int device = 0;
+};
+
+namespace {
+
+int vec_width(int dtype) { return dtype == PRK_FP64 ? 2 : 4; }
+
+int tiles_of(int64_t n, int dtype, int* tx)
+{
+    const int tw = dtype == PRK_FP64 ? prk::tile::Cfg<prk::FP64>::TW : prk::tile::Cfg<prk::FP32C>::TW;
+    const int th = dtype == PRK_FP64 ? prk::tile::Cfg<prk::FP64>::TH : prk::tile::Cfg<prk::FP32C>::TH;
+    *tx = static_cast<int>((n + tw - 1) / tw);
+    return static_cast<int>(((n + th - 1) / th) * *tx);
+}
+
+// Device descriptor and tile-offset tables for a list of grids.
+int build_tables(prk_gb300_batch* b, const std::vector<int>& members, GridDesc** d_desc, int64_t** d_off, int64_t* total)
+{
+    std::vector<GridDesc> desc(members.size());
+    std::vector<int64_t> off(members.size() + 1, 0);
+    for (size_t k = 0; k < members.size(); ++k) {
+        const prk_gb300_grid& g = b->grids[members[k]];
+        GridDesc& d = desc[k];
+        d.n = g.n;
+        d.in[0] = g.in_a;
+        d.in[1] = g.in_b;
+        d.out = g.out;
+        d.pattern = g.pattern;
+        d.R = g.radius;
+        d.tiles = tiles_of(g.n, b->dtype, &d.tiles_x);
+        auto al16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
+        d.vec_ok = (g.n % vec_width(b->dtype) == 0) && al16(g.in_a) && al16(g.in_b) && al16(g.out);
+        off[k + 1] = off[k] + d.tiles;
+    }
+    *total = off.back();
+    cudaError_t e;
+    if ((e = cudaMalloc(d_desc, sizeof(GridDesc) * std::max<size_t>(desc.size(), 1))) != cudaSuccess ||
+        (e = cudaMalloc(d_off, sizeof(int64_t) * off.size())) != cudaSuccess) {
+        cudaGetLastError();
+        return err(PRK_ERR_NOMEM, "batch: device table allocation failed");
+    }
+    if ((e = cudaMemcpy(*d_desc, desc.data(), sizeof(GridDesc) * desc.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(*d_off, off.data(), sizeof(int64_t) * off.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cuda_err(e, "batch: table upload");
+    return PRK_OK;
+}
+
+cudaError_t launch_group(const prk_gb300_batch* b, const GridDesc* desc, const int64_t* off, int ngrids, int64_t total,
+                         int depth, int slot, int parity, cudaStream_t s)
+{
+    prk::batch::Launch L{desc, off, ngrids, total, b->d_queue + slot, parity, b->ctas, s};
+    return b->dtype == PRK_FP64 ? prk::batch::launch_fp64(depth, L) : prk::batch::launch_fp32c(depth, L);
+}
+
+int launches_of(const prk_gb300_batch* b, int iterations)
+{
+    int total = 0;
+    for (const Group& g : b->groups) total += (iterations + g.depth - 1) / g.depth + 2;  // remainder split in powers of 2
+    return total;
+}
+
+// The timed part of a run: every group's launches for `iterations` applications. Slots 1.. of the
+// queue; group parities start at 1 (after the warm-up launch).
+int enqueue_timed(prk_gb300_batch* b, int iterations, cudaStream_t s, std::vector<int>* parity_out)
+{
+    int slot = 1;
+    parity_out->assign(b->groups.size(), 1);
+    for (size_t gi = 0; gi < b->groups.size(); ++gi) {
+        Group& g = b->groups[gi];
+        int parity = 1, left = iterations;
+        while (left > 0) {
+            int d = g.depth;
+            while (d > left) d >>= 1;
+            if (slot >= b->queue_slots) return err(PRK_ERR_STATE, "batch: more launches than queue slots");
+            cudaError_t e = launch_group(b, g.d_desc, g.d_off, static_cast<int>(g.members.size()), g.total, d, slot++, parity, s);
+            if (e != cudaSuccess) return cuda_err(e, "batch launch");
+            parity ^= 1;
+            left -= d;
+        }
+        (*parity_out)[gi] = parity;
+    }
+    return PRK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int prk_gb300_batch_create(const prk_gb300_grid* grids, int count, int dtype, int flags, prk_gb300_batch** out)
+{
+    if (!out) return err(PRK_ERR_ARG, "batch: null output handle");
+    *out = nullptr;
+    if (!grids || count < 1) return err(PRK_ERR_ARG, "batch: need at least one grid");
+    if (dtype != PRK_FP64 && dtype != PRK_FP32C) return err(PRK_ERR_ARG, "batch: dtype is not PRK_FP64 or PRK_FP32C");
+    int depth = (flags >> 8) & 0xFF;
+    if (depth == 0) depth = 1;
+    if (!prk::tma_depth_ok(depth)) return err(PRK_ERR_ARG, "batch: temporal depth is not 1, 2, 4 or 8");
+    for (int k = 0; k < count; ++k) {
+        const prk_gb300_grid& g = grids[k];
+        if ((g.pattern != PRK_STAR && g.pattern != PRK_GRID) || g.radius < 1 || g.radius > prk::RMAX || g.n < 1 ||
+            2 * static_cast<int64_t>(g.radius) + 1 > g.n || g.n > prk::NMAX)
+            return err(PRK_ERR_ARG, "batch: a grid has a bad pattern, radius or n");
+        if (!g.in_a || !g.in_b || !g.out) return err(PRK_ERR_ARG, "batch: a grid has a null buffer");
+    }
+    std::unique_ptr<prk_gb300_batch> b(new prk_gb300_batch);
+    b->dtype = dtype;
+    b->grids.assign(grids, grids + count);
+    b->final_in.assign(count, 0);
+    if (cudaError_t e = cudaGetDevice(&b->device)) return cuda_err(e, "cudaGetDevice");
+
+    // group by temporal depth (tuned per grid, or one fixed depth)
+    std::map<int, std::vector<int>> by_depth;
+    for (int k = 0; k < count; ++k) {
+        int d = depth;
+        if (flags & PRK_BATCH_TUNED) {
+            prk_gb300_tuning t{};
+            if (int rc = prk_gb300_tune(grids[k].pattern, grids[k].radius, grids[k].n, dtype, PRK_TUNE_BATCH, &t)) return rc;
+            d = t.depth;
+        }
+        by_depth[d].push_back(k);
+    }
+    for (auto& kv : by_depth) {
+        Group g;
+        g.depth = kv.first;
+        g.members = kv.second;
+        if (int rc = build_tables(b.get(), g.members, &g.d_desc, &g.d_off, &g.total)) return rc;
+        b->groups.push_back(std::move(g));
+    }
+    std::vector<int> all(count);
+    for (int k = 0; k < count; ++k) all[k] = k;
+    if (int rc = build_tables(b.get(), all, &b->d_all, &b->d_all_off, &b->all_total)) return rc;
+
+    int sms = 0, per = 0;
+    if (cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device)) return cuda_err(e, "device query");
+    per = dtype == PRK_FP64 ? prk::batch::ctas_per_sm_fp64(1) : prk::batch::ctas_per_sm_fp32c(1);
+    b->ctas = sms * std::max(per, 1);
+    b->queue_slots = 4096;
+    if (cudaMalloc(&b->d_queue, sizeof(unsigned long long) * b->queue_slots) != cudaSuccess) {
+        cudaGetLastError();
+        return err(PRK_ERR_NOMEM, "batch: queue allocation failed");
+    }
+    *out = b.release();
+    return PRK_OK;
+}
+
+int prk_gb300_batch_run(prk_gb300_batch* b, int iterations, int flags, double* elapsed_s, void* stream)
+{
+    if (!b) return err(PRK_ERR_ARG, "batch: null handle");
+    if (iterations < 1) return err(PRK_ERR_ARG, "iterations must be >= 1");
+    if (launches_of(b, iterations) + 1 > b->queue_slots) return err(PRK_ERR_LIMIT, "batch: too many launches for one run");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaStream_t own = nullptr;
+    const bool graph = (flags & PRK_RUN_GRAPH) != 0;
+    if (graph && !s) {
+        if (cudaError_t e = cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking)) return cuda_err(e, "cudaStreamCreate");
+        s = own;
+        cudaDeviceSynchronize();  // order the private stream after prior legacy-stream work
+    }
+    int rc = PRK_OK;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    std::vector<int> parity;
+    do {
+        cudaError_t e;
+        if ((e = cudaEventCreate(&e0)) != cudaSuccess || (e = cudaEventCreate(&e1)) != cudaSuccess) { rc = cuda_err(e, "cudaEventCreate"); break; }
+        // application 0 (untimed warm-up): one depth-1 launch over every grid, queue slot 0
+        if ((e = cudaMemsetAsync(b->d_queue, 0, sizeof(unsigned long long) * b->queue_slots, s)) != cudaSuccess) { rc = cuda_err(e, "queue reset"); break; }
+        if ((e = launch_group(b, b->d_all, b->d_all_off, static_cast<int>(b->grids.size()), b->all_total, 1, 0, 0, s)) != cudaSuccess) { rc = cuda_err(e, "batch warm-up launch"); break; }
+        if (graph) {
+            cudaGraphExec_t ge = nullptr;
+            auto it = b->graphs.find(iterations);
+            if (it == b->graphs.end()) {
+                cudaGraph_t g = nullptr;
+                if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) { rc = cuda_err(e, "cudaStreamBeginCapture"); break; }
+                rc = cudaMemsetAsync(b->d_queue + 1, 0, sizeof(unsigned long long) * (b->queue_slots - 1), s) == cudaSuccess
+                         ? enqueue_timed(b, iterations, s, &parity) : err(PRK_ERR_STATE, "queue reset during capture");
+                cudaError_t ec = cudaStreamEndCapture(s, &g);
+                if (rc != PRK_OK) { if (g) cudaGraphDestroy(g); break; }
+                if (ec != cudaSuccess) { rc = cuda_err(ec, "cudaStreamEndCapture"); break; }
+                e = cudaGraphInstantiate(&ge, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) { rc = cuda_err(e, "cudaGraphInstantiate"); break; }
+                if ((e = cudaGraphUpload(ge, s)) != cudaSuccess) { rc = cuda_err(e, "cudaGraphUpload"); cudaGraphExecDestroy(ge); break; }
+                b->graphs[iterations] = ge;
+            } else {
+                ge = it->second;
+                parity.assign(b->groups.size(), 1);
+                for (size_t gi = 0; gi < b->groups.size(); ++gi) {  // same launch sequence as captured
+                    int p = 1, left = iterations;
+                    while (left > 0) {
+                        int d = b->groups[gi].depth;
+                        while (d > left) d >>= 1;
+                        p ^= 1;
+                        left -= d;
+                    }
+                    parity[gi] = p;
+                }
+            }
+            cudaEventRecord(e0, s);
+            if ((e = cudaGraphLaunch(ge, s)) != cudaSuccess) { rc = cuda_err(e, "cudaGraphLaunch"); break; }
+            cudaEventRecord(e1, s);
+        } else {
+            cudaEventRecord(e0, s);
+            if ((rc = enqueue_timed(b, iterations, s, &parity)) != PRK_OK) break;
+            cudaEventRecord(e1, s);
+        }
+        if ((e = cudaEventSynchronize(e1)) != cudaSuccess) { rc = cuda_err(e, "batch run"); break; }
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (elapsed_s) *elapsed_s = ms * 1e-3;
+        for (size_t gi = 0; gi < b->groups.size(); ++gi)
+            for (int k : b->groups[gi].members) b->final_in[k] = parity[gi];
+        rc = prk_gb300_status();
+    } while (false);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (own) {
+        cudaStreamSynchronize(own);
+        cudaStreamDestroy(own);
+    }
+    return rc;
+}
+
+int prk_gb300_batch_final_in(const prk_gb300_batch* b, int index)
+{
+    if (!b || index < 0 || index >= static_cast<int>(b->grids.size())) return PRK_ERR_ARG;
+    return b->final_in[index];
+}
+
+int prk_gb300_batch_norms(prk_gb300_batch* b, double* norms, void* stream)
+{
+    if (!b || !norms) return err(PRK_ERR_ARG, "batch: null handle or norms");
+    for (size_t k = 0; k < b->grids.size(); ++k) {
+        const prk_gb300_grid& g = b->grids[k];
+        if (int rc = prk_gb300_norm(g.radius, g.n, b->dtype, g.out, &norms[k], stream)) return rc;
+    }
+    return PRK_OK;
+}
+
+int prk_gb300_batch_launches(const prk_gb300_batch* b, int iterations)
+{
+    if (!b || iterations < 1) return PRK_ERR_ARG;
+    int total = 0;
+    for (const Group& g : b->groups) {
+        int left = iterations;
+        while (left > 0) {
+            int d = g.depth;
+            while (d > left) d >>= 1;
+            ++total;
+            left -= d;
+        }
+    }
+    return total;
+}
+
+int prk_gb300_batch_destroy(prk_gb300_batch* b)
+{
+    if (!b) return PRK_OK;
+    cudaDeviceSynchronize();
+    for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+    for (Group& g : b->groups) {
+        cudaFree(g.d_desc);
+        cudaFree(g.d_off);
+    }
+    cudaFree(b->d_all);
+    cudaFree(b->d_all_off);
+    cudaFree(b->d_queue);
+    delete b;
+    return PRK_OK;
+}
+
+}  // extern "C"

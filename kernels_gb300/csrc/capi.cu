@@ -105,11 +105,13 @@ int norm_scratch(double** out)
 
 // Kernel selection: 0 = automatic (TMA tiles where eligible), 1 = generic only, 2 = TMA required.
 int g_kernel_choice = 0;
+// Set for the duration of a tuned run whose tuning chose the generic kernels.
+thread_local bool t_force_generic = false;
 
 int launch_one(int pattern, int radius, int64_t n, int dtype, const void* in, void* in_next, void* out, cudaStream_t s)
 {
     prk::StencilCall c{pattern, radius, n, dtype, in, in_next, out, s};
-    const bool tma = g_kernel_choice != 1 && prk::tma_eligible(c);
+    const bool tma = g_kernel_choice != 1 && !t_force_generic && prk::tma_eligible(c);
     if (g_kernel_choice == 2 && !tma) return fail(PRK_ERR_ARG, "the TMA tile kernel was required but the call is not eligible");
     if (tma) {
         DevScratch d;
@@ -247,6 +249,18 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
     if (depth == 0) depth = 1;
     if (!prk::tma_depth_ok(depth)) return fail(PRK_ERR_ARG, "temporal depth %d is not 1, 2, 4 or 8", depth);
     if (!in_a || !out || (!unfused && !in_b)) return fail(PRK_ERR_ARG, "null buffer");
+    bool tuned_generic = false;
+    if ((flags & PRK_RUN_TUNED) && !unfused) {
+        prk_gb300_tuning t{};
+        if (int rc = prk_gb300_tune(pattern, radius, n, dtype, 0, &t)) return rc;
+        depth = t.depth;
+        tuned_generic = t.kernel == 1;
+    }
+    struct GenericScope {  // the tuned choice of the generic kernels holds for this run only
+        bool on;
+        explicit GenericScope(bool g) : on(g) { if (on) t_force_generic = true; }
+        ~GenericScope() { if (on) t_force_generic = false; }
+    } generic_scope(tuned_generic);
     const int64_t ib = prk_gb300_bytes(n, dtype, 0), ob = prk_gb300_bytes(n, dtype, 1);
     if (overlaps(in_a, ib, out, ob) || (!unfused && (overlaps(in_b, ib, out, ob) || overlaps(in_a, ib, in_b, ib))))
         return fail(PRK_ERR_ARG, "buffers overlap");
@@ -262,7 +276,7 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
     int cur = 0;
     {
         prk::StencilCall probe{pattern, radius, n, dtype, in_a, in_b, out, nullptr};
-        if (unfused || g_kernel_choice == 1 || !prk::tma_eligible(probe)) depth = 1;
+        if (unfused || g_kernel_choice == 1 || t_force_generic || !prk::tma_eligible(probe)) depth = 1;
     }
     auto step = [&](cudaStream_t st) -> int {
         if (unfused) {

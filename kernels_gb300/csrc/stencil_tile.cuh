@@ -266,10 +266,14 @@ __device__ __forceinline__ bool tile_has_out(int64_t i0, int64_t j0, int64_t n, 
     return (i0 + th > R) && (i0 < n - R) && (j0 + tw > R) && (j0 < n - R);
 }
 
-// Evaluate one tile held in a stage: STEPS applications, then in_next and out to HBM.
-template <int P, int R, int DT, int STEPS>
+// Evaluate one tile whose `in` (with halo) is in shared memory: STEPS applications, then in_next
+// and out to HBM. GLOBAL_OUT = false: the out tile was loaded into shared memory next to `in` (TMA
+// path); true: out is read from HBM here (batched path). vec_ok: rows are 16-byte aligned and n is a
+// multiple of CPT, so a thread's CPT points move as one vector; otherwise they move one by one.
+template <int P, int R, int DT, int STEPS, bool GLOBAL_OUT = false>
 __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, int64_t i0, int64_t j0, int64_t n,
-                                             bool has_out, void* __restrict__ in_next_v, void* __restrict__ out_v)
+                                             bool has_out, void* __restrict__ in_next_v, void* __restrict__ out_v,
+                                             bool vec_ok = true)
 {
     using G = Geo<DT, R>;
     using C = Cfg<DT>;
@@ -283,8 +287,16 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int c0 = lane * CPT;
     const int64_t gj = j0 + c0;
-    const bool col_ok = gj < n;  // n % CPT == 0: a vector is wholly inside or outside the grid
+    const bool col_ok = gj < n;  // at least the first of the thread's CPT columns is in the grid
     const bool cols_interior = gj >= R && gj + CPT <= n - R;
+    // the out word of point (r, c0 + k), from the smem out tile or from HBM
+    auto load_out = [&](int r, int k) -> uint64_t {
+        if constexpr (GLOBAL_OUT) {
+            return gj + k < n ? static_cast<const uint64_t*>(out_v)[(i0 + r) * n + gj + k] : 0ull;
+        } else {
+            return o_tile[r * C::TW + c0 + k];
+        }
+    };
 
     // ---- FP64 power-of-two stencils: certify the tile for the exact integer route ----
     int unit = fx::NOT_FIXED;
@@ -408,10 +420,17 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
                     nxt[k] = __fadd_rn(s_in[soff + k], 1.0f);
             }
         }
-        st_vec(static_cast<T*>(in_next_v) + gi * n + gj, nxt);
+        T* nx = static_cast<T*>(in_next_v) + gi * n + gj;
+        if (vec_ok) {
+            st_vec(nx, nxt);
+        } else {
+#pragma unroll
+            for (int k = 0; k < CPT; ++k)
+                if (gj + k < n) nx[k] = nxt[k];
+        }
         if (row_out) {
             uint64_t* out = static_cast<uint64_t*>(out_v) + gi * n + gj;
-            if (cols_interior) {
+            if (vec_ok && cols_interior) {
 #pragma unroll
                 for (int k = 0; k < CPT; k += 2) *reinterpret_cast<ulonglong2*>(out + k) = make_ulonglong2(o[k], o[k + 1]);
             } else {
@@ -433,7 +452,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
             uint64_t o[CPT];
             if (row_out) {
 #pragma unroll
-                for (int k = 0; k < CPT; ++k) o[k] = o_tile[r * C::TW + c0 + k];
+                for (int k = 0; k < CPT; ++k) o[k] = load_out(r, k);
                 apply_row(r, o);
             }
             store_row(r, o, row_out);
@@ -447,7 +466,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
             const int64_t gi = i0 + r;
             const bool row_out = col_ok && gi < n && has_out && gi >= R && gi < n - R;
 #pragma unroll
-            for (int k = 0; k < CPT; ++k) o[rr][k] = row_out ? o_tile[r * C::TW + c0 + k] : 0ull;
+            for (int k = 0; k < CPT; ++k) o[rr][k] = row_out ? load_out(r, k) : 0ull;
         }
 #pragma unroll 1
         for (int t = 0; t < STEPS; ++t) {
