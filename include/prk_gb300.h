@@ -97,8 +97,9 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
                   int flags, double* elapsed_s, int* final_in, void* stream);
 
 /* A whole PRK run from host memory, the way Cxx11/stencil-cuda.cu drives it (:193-226): copies
- * h_in and h_out to the device, runs iterations+1 fused applications, copies out (and the final in,
- * when h_in_final != NULL) back, and computes the norm. Allocates and frees its device buffers.
+ * h_in and h_out to the device, runs iterations+1 fused applications with the autotuner's kernel and
+ * temporal depth (PRK_RUN_TUNED), copies out (and the final in, when h_in_final != NULL) back, and
+ * computes the norm. Allocates and frees its device buffers.
  * *elapsed_s (optional) is the whole call's wall time including the copies; *kernel_s (optional)
  * the event time of iterations 1..K. Host buffers may be pageable or pinned. */
 int prk_gb300_run_host(int pattern, int radius, int64_t n, int dtype, int iterations, const void* h_in, void* h_out,

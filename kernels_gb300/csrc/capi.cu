@@ -378,7 +378,7 @@ int prk_gb300_run_host(int pattern, int radius, int64_t n, int dtype, int iterat
             (ce = cudaMemcpy(d[2], h_out, ob, cudaMemcpyHostToDevice)) != cudaSuccess) { rc = cuda_fail(ce, "host to device copy"); break; }
         int fin = 0;
         double ks = 0.0;
-        if ((rc = prk_gb300_run(pattern, radius, n, dtype, iterations, d[0], d[1], d[2], 0, &ks, &fin, nullptr)) != PRK_OK) break;
+        if ((rc = prk_gb300_run(pattern, radius, n, dtype, iterations, d[0], d[1], d[2], PRK_RUN_TUNED, &ks, &fin, nullptr)) != PRK_OK) break;
         if ((ce = cudaMemcpy(h_out, d[2], ob, cudaMemcpyDeviceToHost)) != cudaSuccess) { rc = cuda_fail(ce, "device to host copy"); break; }
         if (h_in_final && (ce = cudaMemcpy(h_in_final, d[fin], ib, cudaMemcpyDeviceToHost)) != cudaSuccess) { rc = cuda_fail(ce, "device to host copy"); break; }
         if (norm && (rc = prk_gb300_norm(radius, n, dtype, d[2], norm, nullptr)) != PRK_OK) break;
