@@ -202,6 +202,11 @@ int prk_gb300_batch_launches(const prk_gb300_batch* batch, int iterations);
 
 int prk_gb300_batch_destroy(prk_gb300_batch* batch);
 
+/* Failure-path self-test: runs a kernel whose bounded mbarrier wait runs out by construction (a
+ * barrier nobody arrives on, a short poll limit) and returns what prk_gb300_status reports then:
+ * PRK_ERR_TIMEOUT when the timeout path works. The GPU stays usable; nothing faults or hangs. */
+int prk_gb300_selftest_timeout(void);
+
 /* Bytes one buffer of the given role needs: role 0 = in / in_next, role 1 = out. */
 int64_t prk_gb300_bytes(int64_t n, int dtype, int role);
 

@@ -33,6 +33,7 @@ SIGNATURES: dict[str, tuple] = {
     "prk_gb300_run_host": (_int, [_int, _int, _i64, _int, _int, _vp, _vp, _vp, _pd, _pd, _pd]),
     "prk_gb300_config": (_int, [_int, _int]),
     "prk_gb300_status": (_int, []),
+    "prk_gb300_selftest_timeout": (_int, []),
     "prk_gb300_tune": (_int, [_int, _int, _i64, _int, _int, C.c_void_p]),
     "prk_gb300_batch_create": (_int, [C.c_void_p, _int, _int, _int, C.c_void_p]),
     "prk_gb300_batch_run": (_int, [_vp, _int, _int, _pd, _vp]),

@@ -5,8 +5,10 @@ case. The cases are seeded synthetic PRK fields (in = i+j, out = 0), the same sh
           PRK GFLOP/s, algorithmic HBM GB/s and its fraction of the measured peak, the norm check,
           and the FP32C relative error against the FP64 result (bit-identical to the reference's)
   large   star R=4, FP32C at n = 65536 and FP64 at n = 46000, 200 iterations, tuned depth
+  batch   the seeded 256-grid batch (kernels_gb300.workloads), FP64 and FP32C, one CUDA graph, tuned
+          depth per grid (or --depth D for every grid)
 
-  python -m kernels_gb300.configs sweep|large [--n N] [--iterations K] [--radii 1,2,...]
+  python -m kernels_gb300.configs sweep|large|batch [--n N] [--iterations K] [--radii 1,2,...] [--depth D]
 """
 from __future__ import annotations
 
@@ -85,10 +87,37 @@ def run_pair(torch, pattern, r, n64, n32, iterations):
     print(json.dumps(rec32), flush=True)
 
 
+def run_batch(torch, iterations: int, depth: int | None, count: int):
+    from kernels_gb300.workloads import batch_specs
+    specs = batch_specs(count)
+    for name, dt in (("fp64", kg.FP64), ("fp32c", kg.FP32C)):
+        grids = []
+        for p, r, n in specs:
+            a, b, o = kg.alloc(n, dt)
+            kg.init(a, o)
+            grids.append((p, r, a, b, o))
+        bt = kg.Batch(grids, depth=depth, tuned=depth is None)
+        bt.run(iterations, graph=True)  # tuning, capture, warm-up
+        for p, r, a, b, o in grids:
+            kg.init(a, o)
+        t = bt.run(iterations, graph=True)
+        norms = bt.norms()
+        fl = sum(kg.flops(p, r, n) for p, r, n in specs) * iterations
+        print(json.dumps({"config": "batch", "grids": len(specs), "dtype": name, "iterations": iterations,
+                          "depth": depth or "tuned", "gflops": round(fl / t / 1e9, 3), "seconds": round(t, 5),
+                          "launches": bt.launches(iterations),
+                          "norms_ok": all(abs(x - 2.0 * (iterations + 1)) <= 1e-8 for x in norms)}), flush=True)
+        bt.close()
+        del grids
+        torch.cuda.empty_cache()
+
+
 def main() -> None:
     import torch
     ap = argparse.ArgumentParser()
-    ap.add_argument("which", choices=["sweep", "large"])
+    ap.add_argument("which", choices=["sweep", "large", "batch"])
+    ap.add_argument("--depth", type=int, default=None)
+    ap.add_argument("--grids", type=int, default=256)
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--iterations", type=int, default=None)
     ap.add_argument("--radii", default="1,2,3,4,5")
@@ -100,9 +129,11 @@ def main() -> None:
         for name in args.patterns.split(","):
             for r in (int(x) for x in args.radii.split(",")):
                 run_pair(torch, kg.pattern_of(name), r, n, n, k)
-    else:
+    elif args.which == "large":
         k = args.iterations or 200
         run_pair(torch, kg.STAR, 4, args.n or 46000, 65536, k)
+    else:
+        run_batch(torch, args.iterations or 50, args.depth, args.grids)
 
 
 if __name__ == "__main__":

@@ -175,6 +175,16 @@ int prk_gb300_config(int key, int value)
 
 int prk_gb300_status(void) { return check_status(); }
 
+int prk_gb300_selftest_timeout(void)
+{
+    if (int rc = check_status()) return rc;  // start from a clear status word
+    DevScratch d;
+    if (int rc = dev_scratch(&d)) return rc;
+    PRK_CUDA(prk::launch_wait_selftest(d.status, nullptr), "self-test launch");
+    PRK_CUDA(cudaDeviceSynchronize(), "self-test");
+    return check_status();
+}
+
 int64_t prk_gb300_bytes(int64_t n, int dtype, int role)
 {
     if (n < 1 || (dtype != PRK_FP64 && dtype != PRK_FP32C)) return -1;

@@ -31,6 +31,8 @@ inline int64_t out_elem_bytes(int dtype) { return 8; }
 // `steps` consecutive applications per launch (temporal depth 1, 2, 4 or 8). `status` is a device
 // word; bit 0 is set if a bounded wait gave up.
 bool tma_eligible(const StencilCall& c);
+// Launches a kernel whose bounded mbarrier wait runs out by construction (tile_host.cu).
+cudaError_t launch_wait_selftest(unsigned* status, cudaStream_t s);
 bool tma_depth_ok(int steps);
 cudaError_t launch_stencil_tma(const StencilCall& c, int steps, unsigned* status);
 

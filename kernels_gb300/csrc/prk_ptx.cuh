@@ -52,9 +52,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
 // hardware-defined interval, so the limit corresponds to seconds, far beyond any TMA completion.
 constexpr uint32_t MBAR_SPIN_LIMIT = 1u << 24;
 
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t limit = MBAR_SPIN_LIMIT)
 {
-    for (uint32_t it = 0; it < MBAR_SPIN_LIMIT; ++it)
+    for (uint32_t it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }

@@ -45,6 +45,32 @@ cudaError_t make_map(CUtensorMap* map, const void* base, int64_t n, int elem_byt
 
 }  // namespace
 
+namespace {
+
+// A wait that must run out: the barrier expects one arrival that nobody makes. Every thread gives up
+// after `limit` polls, and the CTA reports through the status word exactly as a stalled tile load
+// would. No copy is in flight, so returning is safe.
+__global__ void k_wait_timeout_selftest(unsigned* status, uint32_t limit)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const bool ok = mbar_wait_bounded(&bar, 0, limit);
+    __syncthreads();
+    if (!ok && threadIdx.x == 0) atomicOr(status, 1u);
+}
+
+}  // namespace
+
+cudaError_t launch_wait_selftest(unsigned* status, cudaStream_t s)
+{
+    k_wait_timeout_selftest<<<1, 64, 0, s>>>(status, 1000);
+    return cudaGetLastError();
+}
+
 bool tma_eligible(const StencilCall& c)
 {
     if (!c.in_next) return false;  // the reference-operator form (no in_next) uses the generic kernel

@@ -154,3 +154,18 @@ def test_rejected_calls_raise(cuda):
     small = kg.alloc(4)
     with pytest.raises(kg.PrkError):
         kg.apply(kg.GRID, 2, small[0], small[2])  # 2R+1 > n
+
+
+def test_bounded_wait_reports_timeout_and_gpu_stays_usable(cuda):
+    """A kernel waits on an mbarrier nobody arrives on; its bounded wait gives up, the status word
+    turns into PRK_ERR_TIMEOUT, and the next stencil call still works."""
+    from kernels_gb300 import _lib
+    lib = _lib.load()
+    assert lib.prk_gb300_selftest_timeout() == -4
+    assert b"gave up" in lib.prk_gb300_last_error()
+    kg.status()  # cleared
+    n = 64
+    in_a, in_b, out = kg.alloc(n)
+    kg.init(in_a, out)
+    kg.run(kg.STAR, 2, 3, in_a, in_b, out)
+    assert abs(kg.norm(2, out) - 8.0) <= 1e-8
