@@ -240,6 +240,75 @@ __device__ __forceinline__ void fx_points(const int64_t* v, int ld, I (&S)[CPT])
     }
 }
 
+// N consecutive floats from 8-byte-aligned shared memory (float2 loads).
+template <int N>
+__device__ __forceinline__ void ld_seg2(const float* p, float (&v)[N])
+{
+    static_assert(N % 2 == 0, "segment is whole float2 vectors");
+#pragma unroll
+    for (int q = 0; q < N / 2; ++q) {
+        const float2 t = reinterpret_cast<const float2*>(p)[q];
+        v[2 * q] = t.x;
+        v[2 * q + 1] = t.y;
+    }
+}
+
+// The integer route in FP32: every value of the tile is an integer below 2^20, so the differences,
+// the products by the small integer coefficients and every partial sum are integers below 2^24 and
+// FP32 arithmetic is exact. Sum of c * (V[p+d] - V[p-d]) for CPT points; v points at V(r, c0).
+template <int P, int R, int CPT, int RA>
+__device__ __forceinline__ void fexact_points(const float* v, int ld, float (&S)[CPT])
+{
+    constexpr int SEG = CPT + 2 * RA;
+#pragma unroll
+    for (int k = 0; k < CPT; ++k) S[k] = 0.0f;
+    {
+        float m0[SEG];
+        ld_seg2<SEG>(v - RA, m0);
+#pragma unroll
+        for (int dc = 1; dc <= R; ++dc) {
+            const float cc = static_cast<float>(coef<P, R>(dc, 0));
+#pragma unroll
+            for (int k = 0; k < CPT; ++k) S[k] = __fmaf_rn(cc, __fsub_rn(m0[k + RA + dc], m0[k + RA - dc]), S[k]);
+        }
+    }
+#pragma unroll
+    for (int dr = 1; dr <= R; ++dr) {
+        if constexpr (P == STAR) {
+            float up[CPT], dn[CPT];
+            ld_seg2<CPT>(v + dr * ld, up);
+            ld_seg2<CPT>(v - dr * ld, dn);
+            const float cc = static_cast<float>(coef<P, R>(0, dr));
+#pragma unroll
+            for (int k = 0; k < CPT; ++k) S[k] = __fmaf_rn(cc, __fsub_rn(up[k], dn[k]), S[k]);
+        } else {
+            float up[SEG], dn[SEG];
+            ld_seg2<SEG>(v + dr * ld - RA, up);
+            ld_seg2<SEG>(v - dr * ld - RA, dn);
+#pragma unroll
+            for (int dc = -R; dc <= R; ++dc) {
+                const int c = coef<P, R>(dc, dr);
+                if (c != 0) {
+#pragma unroll
+                    for (int k = 0; k < CPT; ++k)
+                        S[k] = __fmaf_rn(static_cast<float>(c), __fsub_rn(up[k + RA + dc], dn[k + RA - dc]), S[k]);
+                }
+            }
+        }
+    }
+}
+
+// binary64 encoding of f * 2^adj for an integer-valued f (|f| < 2^24): exponent rebias and a
+// mantissa shift, no conversion instruction (those run on the binary64 pipe).
+__device__ __forceinline__ uint64_t f2d(float f, int adj)
+{
+    const uint32_t u = __float_as_uint(f);
+    const uint64_t mag = u & 0x7FFFFFFFu;
+    const uint64_t d = (static_cast<uint64_t>(u & 0x80000000u) << 32) |
+                       ((mag + (static_cast<uint64_t>(896 + adj) << 23)) << 29);
+    return mag == 0 ? 0ull : d;
+}
+
 // binary64 encoding of x * 2^unit for a 32-bit x (exact).
 __device__ __forceinline__ uint64_t from_fixed32(int32_t x, int unit)
 {
@@ -298,50 +367,73 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
         }
     };
 
-    // ---- FP64 power-of-two stencils: certify the tile for the exact integer route ----
+    // ---- FP64 power-of-two stencils: certify the tile for an exact route ----
+    // First the FP32 route: every value +0 or an integer of magnitude below 2^20 (checked with a few
+    // integer ops and one FP32 round trip, no binary64 instruction). Otherwise the general integer
+    // route (lowest-set-bit classification, int32/int64 arithmetic), otherwise strict binary64.
     int unit = fx::NOT_FIXED;
     bool narrow = false;
+    bool fexact = false;
     if constexpr (EXACT) {
         constexpr int SHIFT = pow2_shift(P, R);
         constexpr long long L1 = pow2_coef_l1(P, R);
         constexpr int PER = (G::ELEMS + THREADS - 1) / THREADS;
-        uint64_t vals[PER];
-        int lo = fx::ZERO_LO, hi = fx::ZERO_HI;
+        static_assert(L1 < 16 && STEPS <= 8, "FP32 route bound: (L1/2) * 2 * (2^20 + 8) < 2^24");
         const uint64_t* raw = reinterpret_cast<const uint64_t*>(s_in);
+        float fv[PER];
+        bool ok = true;
 #pragma unroll
         for (int q = 0; q < PER; ++q) {
             const int idx = threadIdx.x + q * THREADS;
-            vals[q] = idx < G::ELEMS ? raw[idx] : 0ull;
-            int l, h;
-            fx::classify(vals[q], l, h);
-            lo = min(lo, l);
-            hi = max(hi, h);
+            const uint64_t b = idx < G::ELEMS ? raw[idx] : 0ull;
+            const uint32_t hi32 = static_cast<uint32_t>(b >> 32), lo32 = static_cast<uint32_t>(b);
+            const uint32_t e = (hi32 >> 20) & 0x7FFu;
+            const bool small = e >= 1023u && e < 1043u && (lo32 & 0x1FFFFFFFu) == 0u;
+            const float f = __uint_as_float((hi32 & 0x80000000u) | (((hi32 & 0x7FFFFFFFu) - (896u << 20)) << 3) | (lo32 >> 29));
+            const float fr = __fsub_rn(__fadd_rn(f, 12582912.0f), 12582912.0f);  // nearest integer, |f| < 2^22
+            ok = ok && (b == 0ull || (small && fr == f));
+            fv[q] = b == 0ull ? 0.0f : f;
         }
-        lo = __reduce_min_sync(0xffffffffu, lo);
-        hi = __reduce_max_sync(0xffffffffu, hi);
-        if (lane == 0) {
-            s_red[2 * warp] = lo;
-            s_red[2 * warp + 1] = hi;
-        }
-        __syncthreads();
-        lo = s_red[0];
-        hi = s_red[1];
-#pragma unroll
-        for (int w = 1; w < WARPS; ++w) {
-            lo = min(lo, s_red[2 * w]);
-            hi = max(hi, s_red[2 * w + 1]);
-        }
-        unit = fx::certify(lo, hi, SHIFT, L1, STEPS);
-        if (unit != fx::NOT_FIXED) {
-            // int32 arithmetic suffices when every partial sum and every updated value stays below 2^31
-            const int span = hi == fx::ZERO_HI ? 0 : hi + 1 - unit;
-            narrow = span <= 30 && -unit <= 26 &&
-                     ((1ll << span) + static_cast<long long>(STEPS) * (1ll << (-unit))) < (1ll << 31) / L1;
-            int64_t* iv = reinterpret_cast<int64_t*>(s_in);
+        ok = __syncthreads_and(ok) != 0;
+        if (ok) {
+            float* sf = reinterpret_cast<float*>(s_in);
 #pragma unroll
             for (int q = 0; q < PER; ++q) {
                 const int idx = threadIdx.x + q * THREADS;
-                if (idx < G::ELEMS) iv[idx] = fx::to_fixed(vals[q], unit);
+                if (idx < G::ELEMS) sf[idx] = fv[q];
+            }
+            fexact = true;
+        } else {
+            int lo = fx::ZERO_LO, hi = fx::ZERO_HI;
+            for (int idx = threadIdx.x; idx < G::ELEMS; idx += THREADS) {
+                int l, h;
+                fx::classify(raw[idx], l, h);
+                lo = min(lo, l);
+                hi = max(hi, h);
+            }
+            lo = __reduce_min_sync(0xffffffffu, lo);
+            hi = __reduce_max_sync(0xffffffffu, hi);
+            if (lane == 0) {
+                s_red[2 * warp] = lo;
+                s_red[2 * warp + 1] = hi;
+            }
+            __syncthreads();
+            lo = s_red[0];
+            hi = s_red[1];
+#pragma unroll
+            for (int w = 1; w < WARPS; ++w) {
+                lo = min(lo, s_red[2 * w]);
+                hi = max(hi, s_red[2 * w + 1]);
+            }
+            unit = fx::certify(lo, hi, SHIFT, L1, STEPS);
+            if (unit != fx::NOT_FIXED) {
+                // int32 arithmetic suffices when every partial sum and every updated value stays below 2^31
+                const int span = hi == fx::ZERO_HI ? 0 : hi + 1 - unit;
+                narrow = span <= 30 && -unit <= 26 &&
+                         ((1ll << span) + static_cast<long long>(STEPS) * (1ll << (-unit))) < (1ll << 31) / L1;
+                __syncthreads();  // every thread has read its raw words
+                int64_t* iv = reinterpret_cast<int64_t*>(s_in);
+                for (int idx = threadIdx.x; idx < G::ELEMS; idx += THREADS) iv[idx] = fx::to_fixed(raw[idx], unit);
             }
         }
         __syncthreads();  // every converted word visible
@@ -355,7 +447,13 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
             if constexpr (EXACT) {
                 constexpr int SHIFT = pow2_shift(P, R);
                 const int64_t* v = reinterpret_cast<const int64_t*>(s_in) + soff;
-                if (unit != fx::NOT_FIXED) {
+                if (fexact) {
+                    float S[CPT];
+                    fexact_points<P, R, CPT, G::RA>(reinterpret_cast<const float*>(s_in) + soff, G::SW, S);
+#pragma unroll
+                    for (int k = 0; k < CPT; ++k) o[k] = as_bits(__dadd_rn(as_dbl(o[k]), as_dbl(f2d(S[k], -SHIFT))));
+                    done = true;
+                } else if (unit != fx::NOT_FIXED) {
                     if (narrow) {
                         int32_t S[CPT];
                         fx_points<P, R, CPT, G::RA>(v, G::SW, S);
@@ -398,7 +496,12 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
         T nxt[CPT];
         bool done = false;
         if constexpr (EXACT) {
-            if (unit != fx::NOT_FIXED) {
+            if (fexact) {
+                const float* v = reinterpret_cast<const float*>(s_in) + soff;
+#pragma unroll
+                for (int k = 0; k < CPT; ++k) nxt[k] = as_dbl(f2d(__fadd_rn(v[k], 1.0f), 0));
+                done = true;
+            } else if (unit != fx::NOT_FIXED) {
                 const int64_t* v = reinterpret_cast<const int64_t*>(s_in) + soff;
                 const int64_t one = 1ll << (-unit);
                 if (narrow) {
@@ -474,7 +577,9 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
                 __syncthreads();
                 for (int idx = threadIdx.x; idx < G::ELEMS; idx += THREADS) {
                     if constexpr (DT == FP64) {
-                        if (EXACT && unit != fx::NOT_FIXED)
+                        if (EXACT && fexact)
+                            reinterpret_cast<float*>(s_in)[idx] = __fadd_rn(reinterpret_cast<float*>(s_in)[idx], 1.0f);
+                        else if (EXACT && unit != fx::NOT_FIXED)
                             reinterpret_cast<int64_t*>(s_in)[idx] += (1ll << (-unit));
                         else
                             s_in[idx] = __dadd_rn(s_in[idx], 1.0);
