@@ -169,3 +169,17 @@ def test_bounded_wait_reports_timeout_and_gpu_stays_usable(cuda):
     kg.init(in_a, out)
     kg.run(kg.STAR, 2, 3, in_a, in_b, out)
     assert abs(kg.norm(2, out) - 8.0) <= 1e-8
+
+
+@pytest.mark.parametrize("args", [("10", "1000"), ("10", "200", "20", "grid", "3"), ("10", "200", "20", "star", "5", "--unfused"),
+                                  ("10", "1000", "32", "star", "2", "--dtype", "fp32c", "--graph")])
+def test_cli_driver_validates(cuda, args):
+    """The C++ driver with the reference CLI prints the reference's verdict and rate lines."""
+    import subprocess
+    from pathlib import Path
+    cli = Path(__file__).resolve().parents[1] / "kernels_gb300" / "_build" / "stencil-gb300"
+    res = subprocess.run([str(cli), *args], capture_output=True, text=True, timeout=120)
+    assert res.returncode == 0, res.stdout + res.stderr
+    assert "Solution validates" in res.stdout
+    assert "Rate (MFlops/s): " in res.stdout and "Avg time (s): " in res.stdout
+    assert "L1 norm = 22 Reference L1 norm = 22" in res.stdout
