@@ -99,7 +99,8 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
 /* A whole PRK run from host memory, the way Cxx11/stencil-cuda.cu drives it (:193-226): copies
  * h_in and h_out to the device, runs iterations+1 fused applications with the autotuner's kernel and
  * temporal depth (PRK_RUN_TUNED), copies out (and the final in, when h_in_final != NULL) back, and
- * computes the norm. Allocates and frees its device buffers.
+ * computes the norm. Its device buffers are allocated on first use and kept for later calls (grown
+ * when a larger grid comes); prk_gb300_release frees them. Calls are serialised process-wide.
  * *elapsed_s (optional) is the whole call's wall time including the copies; *kernel_s (optional)
  * the event time of iterations 1..K. Host buffers may be pageable or pinned. */
 int prk_gb300_run_host(int pattern, int radius, int64_t n, int dtype, int iterations, const void* h_in, void* h_out,
@@ -206,6 +207,9 @@ int prk_gb300_batch_destroy(prk_gb300_batch* batch);
  * barrier nobody arrives on, a short poll limit) and returns what prk_gb300_status reports then:
  * PRK_ERR_TIMEOUT when the timeout path works. The GPU stays usable; nothing faults or hangs. */
 int prk_gb300_selftest_timeout(void);
+
+/* Frees the device buffers prk_gb300_run_host keeps on the current device. */
+int prk_gb300_release(void);
 
 /* Bytes one buffer of the given role needs: role 0 = in / in_next, role 1 = out. */
 int64_t prk_gb300_bytes(int64_t n, int dtype, int role);

@@ -103,6 +103,15 @@ int norm_scratch(double** out)
     return PRK_OK;
 }
 
+// Device buffers of prk_gb300_run_host, kept between calls (grown when a larger grid comes) and
+// freed by prk_gb300_release.
+struct HostWorkspace {
+    void* d[3] = {nullptr, nullptr, nullptr};
+    int64_t in_bytes = 0, out_bytes = 0;
+};
+std::mutex g_host_mu;
+std::vector<HostWorkspace> g_host_ws;
+
 // Kernel selection: 0 = automatic (TMA tiles where eligible), 1 = generic only, 2 = TMA required.
 int g_kernel_choice = 0;
 // Set for the duration of a tuned run whose tuning chose the generic kernels.
@@ -373,17 +382,35 @@ int prk_gb300_run_host(int pattern, int radius, int64_t n, int dtype, int iterat
     if (iterations < 1) return fail(PRK_ERR_ARG, "iterations must be >= 1");
     if (!h_in || !h_out) return fail(PRK_ERR_ARG, "h_in and h_out must be non-null");
     const int64_t ib = prk_gb300_bytes(n, dtype, 0), ob = prk_gb300_bytes(n, dtype, 1);
-    void* d[3] = {nullptr, nullptr, nullptr};
+    int dev = 0;
+    PRK_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> lock(g_host_mu);  // one host-buffer run per process at a time
+    if (static_cast<int>(g_host_ws.size()) <= dev) g_host_ws.resize(dev + 1);
+    HostWorkspace& ws = g_host_ws[dev];
     int rc = PRK_OK;
     do {
         cudaError_t ce;
-        if ((ce = cudaMalloc(&d[0], ib)) != cudaSuccess || (ce = cudaMalloc(&d[1], ib)) != cudaSuccess ||
-            (ce = cudaMalloc(&d[2], ob)) != cudaSuccess) {
-            cudaGetLastError();
-            rc = fail(PRK_ERR_NOMEM, "device allocation of %lld bytes failed: %s", static_cast<long long>(2 * ib + ob),
-                      cudaGetErrorString(ce));
-            break;
+        if (ws.in_bytes < ib || ws.out_bytes < ob) {  // grow the cached device buffers
+            for (void*& p : ws.d) {
+                if (p) cudaFree(p);
+                p = nullptr;
+            }
+            ws.in_bytes = ws.out_bytes = 0;
+            if ((ce = cudaMalloc(&ws.d[0], ib)) != cudaSuccess || (ce = cudaMalloc(&ws.d[1], ib)) != cudaSuccess ||
+                (ce = cudaMalloc(&ws.d[2], ob)) != cudaSuccess) {
+                cudaGetLastError();
+                for (void*& p : ws.d) {
+                    if (p) cudaFree(p);
+                    p = nullptr;
+                }
+                rc = fail(PRK_ERR_NOMEM, "device allocation of %lld bytes failed: %s", static_cast<long long>(2 * ib + ob),
+                          cudaGetErrorString(ce));
+                break;
+            }
+            ws.in_bytes = ib;
+            ws.out_bytes = ob;
         }
+        void** d = ws.d;
         if ((ce = cudaMemcpy(d[0], h_in, ib, cudaMemcpyHostToDevice)) != cudaSuccess ||
             (ce = cudaMemcpy(d[2], h_out, ob, cudaMemcpyHostToDevice)) != cudaSuccess) { rc = cuda_fail(ce, "host to device copy"); break; }
         int fin = 0;
@@ -394,10 +421,23 @@ int prk_gb300_run_host(int pattern, int radius, int64_t n, int dtype, int iterat
         if (norm && (rc = prk_gb300_norm(radius, n, dtype, d[2], norm, nullptr)) != PRK_OK) break;
         if (kernel_s) *kernel_s = ks;
     } while (false);
-    for (void* p : d)
-        if (p) cudaFree(p);
     if (elapsed_s) *elapsed_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return rc;
+}
+
+int prk_gb300_release(void)
+{
+    int dev = 0;
+    PRK_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> lock(g_host_mu);
+    if (static_cast<int>(g_host_ws.size()) > dev) {
+        for (void*& p : g_host_ws[dev].d) {
+            if (p) cudaFree(p);
+            p = nullptr;
+        }
+        g_host_ws[dev].in_bytes = g_host_ws[dev].out_bytes = 0;
+    }
+    return PRK_OK;
 }
 
 }  // extern "C"

@@ -89,19 +89,20 @@ int prk_oracle_taps(int pattern, int R, int* dc_out, int* dr_out, double* w_out)
 /* One stencil application over the interior, tiled by t, as an orphaned `omp for` over tiles
  * (stencil_openmp.hpp:2-15). With pattern and R compile-time constants, the unrolled tap loops
  * fold into the same straight-line expression the generator emits. */
-#define DEFINE_APPLY(P, PNAME, RR)                                                                        \
-    static void apply_##PNAME##RR(const int64_t n, const int64_t t, const double* restrict in,           \
-                                  double* restrict out)                                                   \
+#define DEFINE_APPLY_T(P, PNAME, RR, IDX, SUFFIX)                                                          \
+    static void apply_##PNAME##RR##SUFFIX(const int64_t n64, const int64_t t64, const double* restrict in,  \
+                                          double* restrict out)                                            \
     {                                                                                                     \
         const int R = RR;                                                                                 \
+        const IDX n = (IDX)n64, t = (IDX)t64;                                                             \
         _Pragma("omp for collapse(2) schedule(static)")                                                   \
-        for (int64_t it = R; it < n - R; it += t) {                                                       \
-            for (int64_t jt = R; jt < n - R; jt += t) {                                                   \
-                const int64_t iend = (it + t < n - R) ? it + t : n - R;                                   \
-                const int64_t jend = (jt + t < n - R) ? jt + t : n - R;                                   \
-                for (int64_t i = it; i < iend; ++i) {                                                     \
+        for (IDX it = R; it < n - R; it += t) {                                                           \
+            for (IDX jt = R; jt < n - R; jt += t) {                                                       \
+                const IDX iend = (it + t < n - R) ? it + t : n - R;                                       \
+                const IDX jend = (jt + t < n - R) ? jt + t : n - R;                                       \
+                for (IDX i = it; i < iend; ++i) {                                                         \
                     _Pragma("omp simd")                                                                   \
-                    for (int64_t j = jt; j < jend; ++j) {                                                 \
+                    for (IDX j = jt; j < jend; ++j) {                                                     \
                         double s = 0.0;                                                                   \
                         int first = 1;                                                                    \
                         _Pragma("GCC unroll 16")                                                          \
@@ -125,6 +126,17 @@ int prk_oracle_taps(int pattern, int R, int* dc_out, int* dr_out, double* w_out)
                 }                                                                                         \
             }                                                                                             \
         }                                                                                                 \
+    }
+
+/* 32-bit indices below n = 46340, as the reference (prk::get_max_matrix_size, prk_util.h:373-377);
+ * 64-bit above. */
+#define DEFINE_APPLY(P, PNAME, RR)                  \
+    DEFINE_APPLY_T(P, PNAME, RR, int, _i32)         \
+    DEFINE_APPLY_T(P, PNAME, RR, int64_t, _i64)     \
+    static void apply_##PNAME##RR(const int64_t n, const int64_t t, const double* restrict in, double* restrict out) \
+    {                                                                                                     \
+        if (n <= 46340) apply_##PNAME##RR##_i32(n, t, in, out);                                          \
+        else apply_##PNAME##RR##_i64(n, t, in, out);                                                      \
     }
 
 DEFINE_APPLY(PRK_STAR, star, 1)
@@ -151,6 +163,20 @@ static apply_fn select_apply(int pattern, int R)
 
 static void add_one(const int64_t n, const int64_t t, double* restrict in)
 {
+    if (n <= 46340) {  /* 32-bit indices, as the reference */
+        const int ni = (int)n, ti = (int)t;
+        _Pragma("omp for collapse(2) schedule(static)")
+        for (int it = 0; it < ni; it += ti)
+            for (int jt = 0; jt < ni; jt += ti) {
+                const int iend = (it + ti < ni) ? it + ti : ni;
+                const int jend = (jt + ti < ni) ? jt + ti : ni;
+                for (int i = it; i < iend; ++i) {
+                    _Pragma("omp simd")
+                    for (int j = jt; j < jend; ++j) in[i * ni + j] += 1.0;
+                }
+            }
+        return;
+    }
     _Pragma("omp for collapse(2) schedule(static)")
     for (int64_t it = 0; it < n; it += t)
         for (int64_t jt = 0; jt < n; jt += t) {
