@@ -55,6 +55,8 @@ extern "C" {
 /* Temporal depth d in {1, 2, 4, 8}: each launch applies d consecutive applications to a tile held
  * in shared memory (the fused form on TMA-eligible buffers; otherwise depth 1). */
 #define PRK_RUN_DEPTH(d) ((d) << 8)
+/* Tall tiles: 64 rows per TMA tile (8 rows per thread) instead of 32 (4 per thread). */
+#define PRK_RUN_TALL 8
 
 /* One application of the stencil (replaces starR/gridR, stencil_openmp.hpp:1, stencil_cuda.hpp:1):
  *   out[i*n+j] += sum over taps of w * in[(i+dr)*n + (j+dc)]   for R <= i,j < n-R,

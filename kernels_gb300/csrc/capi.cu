@@ -114,8 +114,9 @@ std::vector<HostWorkspace> g_host_ws;
 
 // Kernel selection: 0 = automatic (TMA tiles where eligible), 1 = generic only, 2 = TMA required.
 int g_kernel_choice = 0;
-// Set for the duration of a tuned run whose tuning chose the generic kernels.
+// Set for the duration of a tuned run whose tuning chose the generic kernels, or a tile height.
 thread_local bool t_force_generic = false;
+thread_local int t_tile_rows = 32;
 
 int launch_one(int pattern, int radius, int64_t n, int dtype, const void* in, void* in_next, void* out, cudaStream_t s)
 {
@@ -125,7 +126,7 @@ int launch_one(int pattern, int radius, int64_t n, int dtype, const void* in, vo
     if (tma) {
         DevScratch d;
         if (int rc = dev_scratch(&d)) return rc;
-        PRK_CUDA(prk::launch_stencil_tma(c, 1, d.status), "stencil launch (TMA tiles)");
+        PRK_CUDA(prk::launch_stencil_tma(c, 1, d.status, t_tile_rows), "stencil launch (TMA tiles)");
     } else {
         PRK_CUDA(prk::launch_stencil_generic(c), "stencil launch");
     }
@@ -143,7 +144,7 @@ int launch_steps(int pattern, int radius, int64_t n, int dtype, int steps, const
                     dtype == PRK_FP64 ? 2 : 4);
     DevScratch d;
     if (int rc = dev_scratch(&d)) return rc;
-    PRK_CUDA(prk::launch_stencil_tma(c, steps, d.status), "stencil launch (TMA tiles, temporal)");
+    PRK_CUDA(prk::launch_stencil_tma(c, steps, d.status, t_tile_rows), "stencil launch (TMA tiles, temporal)");
     return PRK_OK;
 }
 
@@ -269,17 +270,28 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
     if (!prk::tma_depth_ok(depth)) return fail(PRK_ERR_ARG, "temporal depth %d is not 1, 2, 4 or 8", depth);
     if (!in_a || !out || (!unfused && !in_b)) return fail(PRK_ERR_ARG, "null buffer");
     bool tuned_generic = false;
+    int rows = (flags & PRK_RUN_TALL) ? 64 : 32;
     if ((flags & PRK_RUN_TUNED) && !unfused) {
         prk_gb300_tuning t{};
         if (int rc = prk_gb300_tune(pattern, radius, n, dtype, 0, &t)) return rc;
         depth = t.depth;
         tuned_generic = t.kernel == 1;
+        if (!tuned_generic) rows = t.tile_rows;
     }
-    struct GenericScope {  // the tuned choice of the generic kernels holds for this run only
-        bool on;
-        explicit GenericScope(bool g) : on(g) { if (on) t_force_generic = true; }
-        ~GenericScope() { if (on) t_force_generic = false; }
-    } generic_scope(tuned_generic);
+    struct TuneScope {  // the tuned kernel family and tile height hold for this run only
+        bool generic;
+        int prev_rows;
+        TuneScope(bool g, int r) : generic(g), prev_rows(t_tile_rows)
+        {
+            if (generic) t_force_generic = true;
+            t_tile_rows = r;
+        }
+        ~TuneScope()
+        {
+            if (generic) t_force_generic = false;
+            t_tile_rows = prev_rows;
+        }
+    } tune_scope(tuned_generic, rows);
     const int64_t ib = prk_gb300_bytes(n, dtype, 0), ob = prk_gb300_bytes(n, dtype, 1);
     if (overlaps(in_a, ib, out, ob) || (!unfused && (overlaps(in_b, ib, out, ob) || overlaps(in_a, ib, in_b, ib))))
         return fail(PRK_ERR_ARG, "buffers overlap");

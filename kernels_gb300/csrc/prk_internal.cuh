@@ -34,7 +34,9 @@ bool tma_eligible(const StencilCall& c);
 // Launches a kernel whose bounded mbarrier wait runs out by construction (tile_host.cu).
 cudaError_t launch_wait_selftest(unsigned* status, cudaStream_t s);
 bool tma_depth_ok(int steps);
-cudaError_t launch_stencil_tma(const StencilCall& c, int steps, unsigned* status);
+// Tile heights the TMA kernels are built for (32 and 64 rows).
+bool tma_rows_ok(int tile_rows);
+cudaError_t launch_stencil_tma(const StencilCall& c, int steps, unsigned* status, int tile_rows = 32);
 
 // kernels_generic.cu: any n, any 8-byte-aligned pointers.
 cudaError_t launch_stencil_generic(const StencilCall& c);

@@ -39,25 +39,29 @@ namespace tile {
 constexpr int THREADS = 256;
 constexpr int WARPS = THREADS / 32;
 
-template <int DT>
+// Tile shape per storage form: TW columns (CPT per lane, one 16-byte vector) by TH rows (TH/8 per
+// warp). TH is the tile-height variant the autotuner chooses between (32: 4 rows per thread; 64: 8).
+template <int DT, int TH_ = 32>
 struct Cfg;
-template <>
-struct Cfg<FP64> {
+template <int TH_>
+struct Cfg<FP64, TH_> {
     using T = double;
-    static constexpr int TW = 64, TH = 32, CPT = 2, VEC = 2;
+    static constexpr int TW = 64, TH = TH_, CPT = 2, VEC = 2;
 };
-template <>
-struct Cfg<FP32C> {
+template <int TH_>
+struct Cfg<FP32C, TH_> {
     using T = float;
-    static constexpr int TW = 128, TH = 32, CPT = 4, VEC = 4;
+    static constexpr int TW = 128, TH = TH_, CPT = 4, VEC = 4;
 };
+constexpr int TH_DEFAULT = 32;
+constexpr int TH_TALL = 64;
 
 constexpr int SMEM_PER_SM = 228 * 1024;
 constexpr int SMEM_PER_CTA_MAX = 227 * 1024;
 
-template <int DT, int R>
+template <int DT, int R, int TH_ = 32>
 struct Geo {
-    using C = Cfg<DT>;
+    using C = Cfg<DT, TH_>;
     using T = typename C::T;
     static constexpr int RA = ((R + C::VEC - 1) / C::VEC) * C::VEC;  // halo columns, 16-byte multiple
     static constexpr int SW = C::TW + 2 * RA;                        // in-tile row length = TMA box x
@@ -339,13 +343,13 @@ __device__ __forceinline__ bool tile_has_out(int64_t i0, int64_t j0, int64_t n, 
 // and out to HBM. GLOBAL_OUT = false: the out tile was loaded into shared memory next to `in` (TMA
 // path); true: out is read from HBM here (batched path). vec_ok: rows are 16-byte aligned and n is a
 // multiple of CPT, so a thread's CPT points move as one vector; otherwise they move one by one.
-template <int P, int R, int DT, int STEPS, bool GLOBAL_OUT = false>
+template <int P, int R, int DT, int STEPS, bool GLOBAL_OUT = false, int TH_ = 32>
 __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, int64_t i0, int64_t j0, int64_t n,
                                              bool has_out, void* __restrict__ in_next_v, void* __restrict__ out_v,
                                              bool vec_ok = true)
 {
-    using G = Geo<DT, R>;
-    using C = Cfg<DT>;
+    using G = Geo<DT, R, TH_>;
+    using C = Cfg<DT, TH_>;
     using T = typename C::T;
     constexpr int CPT = C::CPT;
     constexpr int ROWS = G::ROWS;
@@ -611,24 +615,24 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
 // allows, so that every SM has enough loads in flight; the multi-application kernels hold `out` in
 // registers and run at most four tiles per SM. The strict FP64 form is bound by the binary64 pipe
 // and gets the registers its unrolled tap sequence wants.
-template <int P, int R, int DT, int STEPS>
+template <int P, int R, int DT, int STEPS, int TH_>
 constexpr int min_blocks()
 {
     if (DT == FP64 && !pow2_weights(P, R)) return STEPS == 1 ? 2 : 1;
-    const int b = Geo<DT, R>::CTAS;
+    const int b = Geo<DT, R, TH_>::CTAS;
     return STEPS == 1 ? b : (b < 3 ? b : 3);
 }
 
 // One CTA per tile: blockIdx = (tile column, tile row). The elected thread issues the tile's two TMA
 // loads; every thread waits on the mbarrier with a bounded spin, and on a timeout the CTA flags
 // `status`, waits (again bounded) for the copies to land and returns.
-template <int P, int R, int DT, int STEPS>
-__global__ void __launch_bounds__(THREADS, min_blocks<P, R, DT, STEPS>())
+template <int P, int R, int DT, int STEPS, int TH_>
+__global__ void __launch_bounds__(THREADS, min_blocks<P, R, DT, STEPS, TH_>())
     k_stencil_tile(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ CUtensorMap tm_out,
                    const int64_t n, void* __restrict__ in_next_v, void* __restrict__ out_v, unsigned* __restrict__ status)
 {
-    using G = Geo<DT, R>;
-    using C = Cfg<DT>;
+    using G = Geo<DT, R, TH_>;
+    using C = Cfg<DT, TH_>;
     extern __shared__ __align__(128) unsigned char smem[];
     int* s_red = reinterpret_cast<int*>(smem + G::RED_OFF);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + G::BAR_OFF);
@@ -649,36 +653,36 @@ __global__ void __launch_bounds__(THREADS, min_blocks<P, R, DT, STEPS>())
         mbar_wait_bounded(bar, 0);  // let the copies land before the CTA's shared memory is released
         return;
     }
-    process_tile<P, R, DT, STEPS>(smem, s_red, i0, j0, n, has_out, in_next_v, out_v);
+    process_tile<P, R, DT, STEPS, false, TH_>(smem, s_red, i0, j0, n, has_out, in_next_v, out_v);
 }
 
-template <int P, int R, int DT, int STEPS>
+template <int P, int R, int DT, int STEPS, int TH_>
 cudaError_t launch(const Launch& L)
 {
-    using G = Geo<DT, R>;
-    using C = Cfg<DT>;
-    if (cudaError_t e = cudaFuncSetAttribute(k_stencil_tile<P, R, DT, STEPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM))
+    using G = Geo<DT, R, TH_>;
+    using C = Cfg<DT, TH_>;
+    if (cudaError_t e = cudaFuncSetAttribute(k_stencil_tile<P, R, DT, STEPS, TH_>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM))
         return e;
     const int64_t tx = (L.n + C::TW - 1) / C::TW, ty = (L.n + C::TH - 1) / C::TH;
     if (ty > 65535) return cudaErrorInvalidValue;
     const dim3 grid(static_cast<unsigned>(tx), static_cast<unsigned>(ty));
-    k_stencil_tile<P, R, DT, STEPS><<<grid, THREADS, G::SMEM, L.stream>>>(L.tm_in, L.tm_out, L.n, L.in_next, L.out, L.status);
+    k_stencil_tile<P, R, DT, STEPS, TH_><<<grid, THREADS, G::SMEM, L.stream>>>(L.tm_in, L.tm_out, L.n, L.in_next, L.out, L.status);
     return cudaGetLastError();
 }
 
 // Supported temporal depths; a run of any length is split into launches of these.
 constexpr int MAX_STEPS = 8;
 
-template <int P, int DT>
+template <int P, int DT, int TH_>
 cudaError_t launch_pattern(int R, int steps, const Launch& L)
 {
 #define PRK_TILE_CASE(RR)                                        \
     case RR:                                                     \
         switch (steps) {                                         \
-        case 1: return launch<P, RR, DT, 1>(L);                  \
-        case 2: return launch<P, RR, DT, 2>(L);                  \
-        case 4: return launch<P, RR, DT, 4>(L);                  \
-        case 8: return launch<P, RR, DT, 8>(L);                  \
+        case 1: return launch<P, RR, DT, 1, TH_>(L);             \
+        case 2: return launch<P, RR, DT, 2, TH_>(L);             \
+        case 4: return launch<P, RR, DT, 4, TH_>(L);             \
+        case 8: return launch<P, RR, DT, 8, TH_>(L);             \
         default: return cudaErrorInvalidValue;                   \
         }
     switch (R) {
@@ -692,24 +696,27 @@ cudaError_t launch_pattern(int R, int steps, const Launch& L)
     return cudaErrorInvalidValue;
 }
 
-// Tile geometry for the host: box sizes of the two tensor maps.
-inline void boxes(int dtype, int R, int* in_x, int* in_y, int* out_x, int* out_y)
+// Tile geometry for the host: box sizes of the two tensor maps for tile height th.
+inline void boxes(int dtype, int R, int th, int* in_x, int* in_y, int* out_x, int* out_y)
 {
     const int vec = dtype == FP64 ? 2 : 4;
     const int ra = ((R + vec - 1) / vec) * vec;
     const int tw = dtype == FP64 ? Cfg<FP64>::TW : Cfg<FP32C>::TW;
-    const int th = dtype == FP64 ? Cfg<FP64>::TH : Cfg<FP32C>::TH;
     *in_x = tw + 2 * ra;
     *in_y = th + 2 * R;
     *out_x = tw;
     *out_y = th;
 }
 
-// Per-translation-unit entry points (tile_*.cu).
+// Per-translation-unit entry points (tile_*.cu), one per storage form, pattern and tile height.
 cudaError_t launch_fp64_star(int R, int steps, const Launch& L);
 cudaError_t launch_fp64_grid(int R, int steps, const Launch& L);
 cudaError_t launch_fp32c_star(int R, int steps, const Launch& L);
 cudaError_t launch_fp32c_grid(int R, int steps, const Launch& L);
+cudaError_t launch_fp64_star_tall(int R, int steps, const Launch& L);
+cudaError_t launch_fp64_grid_tall(int R, int steps, const Launch& L);
+cudaError_t launch_fp32c_star_tall(int R, int steps, const Launch& L);
+cudaError_t launch_fp32c_grid_tall(int R, int steps, const Launch& L);
 
 }  // namespace tile
 }  // namespace prk

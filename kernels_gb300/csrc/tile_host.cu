@@ -81,12 +81,14 @@ bool tma_eligible(const StencilCall& c)
 
 bool tma_depth_ok(int steps) { return steps == 1 || steps == 2 || steps == 4 || steps == 8; }
 
-cudaError_t launch_stencil_tma(const StencilCall& c, int steps, unsigned* status)
+bool tma_rows_ok(int tile_rows) { return tile_rows == tile::TH_DEFAULT || tile_rows == tile::TH_TALL; }
+
+cudaError_t launch_stencil_tma(const StencilCall& c, int steps, unsigned* status, int tile_rows)
 {
-    if (!tma_depth_ok(steps)) return cudaErrorInvalidValue;
+    if (!tma_depth_ok(steps) || !tma_rows_ok(tile_rows)) return cudaErrorInvalidValue;
     tile::Launch L{};
     int ix, iy, ox, oy;
-    tile::boxes(c.dtype, c.R, &ix, &iy, &ox, &oy);
+    tile::boxes(c.dtype, c.R, tile_rows, &ix, &iy, &ox, &oy);
     if (cudaError_t e = make_map(&L.tm_in, c.in, c.n, c.dtype == FP64 ? 8 : 4, ix, iy)) return e;
     if (cudaError_t e = make_map(&L.tm_out, c.out, c.n, 8, ox, oy)) return e;
     L.n = c.n;
@@ -94,8 +96,13 @@ cudaError_t launch_stencil_tma(const StencilCall& c, int steps, unsigned* status
     L.out = c.out;
     L.status = status;
     L.stream = c.stream;
-    if (c.dtype == FP64) return c.pattern == STAR ? tile::launch_fp64_star(c.R, steps, L) : tile::launch_fp64_grid(c.R, steps, L);
-    return c.pattern == STAR ? tile::launch_fp32c_star(c.R, steps, L) : tile::launch_fp32c_grid(c.R, steps, L);
+    const bool tall = tile_rows == tile::TH_TALL;
+    if (c.dtype == FP64) {
+        if (c.pattern == STAR) return tall ? tile::launch_fp64_star_tall(c.R, steps, L) : tile::launch_fp64_star(c.R, steps, L);
+        return tall ? tile::launch_fp64_grid_tall(c.R, steps, L) : tile::launch_fp64_grid(c.R, steps, L);
+    }
+    if (c.pattern == STAR) return tall ? tile::launch_fp32c_star_tall(c.R, steps, L) : tile::launch_fp32c_star(c.R, steps, L);
+    return tall ? tile::launch_fp32c_grid_tall(c.R, steps, L) : tile::launch_fp32c_grid(c.R, steps, L);
 }
 
 }  // namespace prk

@@ -1,9 +1,9 @@
 // The autotuner (prk_gb300_tune): times the candidate kernel configurations for a (pattern, radius,
 // n, dtype) on scratch buffers and keeps the fastest in memory and in a JSON-lines cache file.
 //
-// Candidates, single grid: the TMA tile kernels at temporal depth 1, 2, 4 and 8 (when the shape
-// allows TMA: n a multiple of the vector width) and the generic kernels. Batched grids: the batched
-// kernel at depth 1, 2, 4 and 8. Every candidate computes the same bits (FP64) or stays within the
+// Candidates, single grid: the TMA tile kernels with tiles of 32 and of 64 rows (4 or 8 rows per
+// thread) at temporal depth 1, 2, 4 and 8 (when the shape allows TMA: n a multiple of the vector
+// width), and the generic kernels. Batched grids: the batched kernel at depth 1, 2, 4 and 8. Every candidate computes the same bits (FP64) or stays within the
 // FP32C bound, so the choice affects speed only.
 #include <cstdio>
 #include <cstdlib>
@@ -168,18 +168,21 @@ extern "C" int prk_gb300_tune(int pattern, int radius, int64_t n, int dtype, int
     const int depths[4] = {1, 2, 4, 8};
     const int prev = prk_gb300_config(PRK_CFG_KERNEL, 0);
     int rc = PRK_OK;
-    for (int d : depths) {
-        double sec = 0.0;
-        if (batch) {
-            rc = time_batch(pattern, radius, m, dtype, d, s, &sec);
-        } else {
-            if (!tma_shape && d > 1) continue;
-            rc = time_run(pattern, radius, m, dtype, PRK_RUN_DEPTH(d), s, &sec);
-        }
-        if (rc) break;
-        if (sec < best.seconds_per_application) {
-            best = prk_gb300_tuning{d, (batch || !tma_shape) ? 1 : 2, th, tw, cpt, sec, 0};
-            if (batch) best.kernel = 3;
+    for (int tall = 0; tall < 2 && !rc; ++tall) {
+        if (tall && (batch || !tma_shape)) break;  // the tall tiles exist for the TMA kernels only
+        for (int d : depths) {
+            double sec = 0.0;
+            if (batch) {
+                rc = time_batch(pattern, radius, m, dtype, d, s, &sec);
+            } else {
+                if (!tma_shape && d > 1) continue;
+                rc = time_run(pattern, radius, m, dtype, PRK_RUN_DEPTH(d) | (tall ? PRK_RUN_TALL : 0), s, &sec);
+            }
+            if (rc) break;
+            if (sec < best.seconds_per_application) {
+                best = prk_gb300_tuning{d, (batch || !tma_shape) ? 1 : 2, tall ? 64 : th, tw, cpt, sec, 0};
+                if (batch) best.kernel = 3;
+            }
         }
     }
     if (!rc && !batch && tma_shape) {  // the generic kernels, depth 1

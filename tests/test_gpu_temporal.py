@@ -80,3 +80,29 @@ def test_bad_depth_rejected(cuda):
         kg.apply_steps(kg.STAR, 2, 3, in_a, out, in_b)
     with pytest.raises(kg.PrkError):
         kg.run(kg.STAR, 2, 4, in_a, in_b, out, depth=16)
+
+
+@pytest.mark.parametrize("pattern,r", ALL)
+@pytest.mark.parametrize("depth", [1, 8])
+def test_tall_tiles_fp64_bit_exact(cuda, pattern, r, depth):
+    """The 64-row tile variant (8 rows per thread) gives the same bits as the reference."""
+    n, k = 330, 9
+    _, ref = po.run(pattern, r, n, k)
+    in_a, in_b, out = kg.alloc(n, kg.FP64)
+    kg.init(in_a, out)
+    kg.run(pattern, r, k, in_a, in_b, out, depth=depth, tall=True)
+    assert np.array_equal(out.cpu().numpy().view(np.uint64), ref.view(np.uint64))
+
+
+@pytest.mark.parametrize("pattern", [kg.STAR, kg.GRID])
+@pytest.mark.parametrize("r", [1, 3, 5])
+def test_tall_tiles_fp32c_bound(cuda, pattern, r):
+    n, k = 516, 9
+    _, ref = po.run(pattern, r, n, k)
+    in_a, in_b, out = kg.alloc(n, kg.FP32C)
+    kg.init(in_a, out)
+    kg.run(pattern, r, k, in_a, in_b, out, depth=4, tall=True)
+    got = out.cpu().numpy().astype(np.float64)
+    got = got[..., 0] + got[..., 1]
+    inner = (slice(r, n - r), slice(r, n - r))
+    assert (np.abs(got[inner] - ref[inner]) / np.abs(ref[inner])).max() <= 1e-6
