@@ -12,6 +12,20 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
+@pytest.fixture(scope="session", autouse=True)
+def native_build():
+    """Build libprk_gb300.so, the driver and the oracle libraries once when they are missing (nvcc
+    cross-compiles for sm_103a without a GPU)."""
+    lib = ROOT / "kernels_gb300" / "_build" / "libprk_gb300.so"
+    if not lib.exists():
+        from kernels_gb300 import build
+        build.build()
+    oracle_lib = ROOT / "oracle" / "_build" / "liboracle.so"
+    if not oracle_lib.exists():
+        import subprocess
+        subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "all"], check=True)
+
+
 @pytest.fixture(scope="session")
 def golden():
     import json
