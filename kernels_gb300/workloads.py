@@ -1,4 +1,5 @@
-"""Seeded synthetic workloads for the stencil configurations (no external dataset exists for PRK).
+"""Seeded synthetic workloads for the stencil configurations (no external dataset exists for PRK), and
+the split of a batch across ranks (its grids are independent, so ranks share no data).
 
 batch_specs(): the batched configuration: 256 independent grids with n log-uniform in [128, 4096],
 radius uniform in {1, 2, 3, 4}, star or grid 50/50, from a fixed seed. Every grid starts from the
@@ -11,6 +12,22 @@ import math
 import numpy as np
 
 BATCH_SEED = 20260101
+
+
+def shard(items: list, rank: int, world: int) -> list[int]:
+    """Indices of the items rank `rank` of `world` owns: a greedy split by work (n^2 per grid, largest
+    first, each to the least-loaded rank), so that ranks finish together. Every index goes to exactly
+    one rank and every rank computes the same split without talking to the others."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("bad rank or world size")
+    order = sorted(range(len(items)), key=lambda k: (-items[k][2] ** 2, k))
+    load = [0] * world
+    owner = [0] * len(items)
+    for k in order:
+        r = min(range(world), key=lambda q: (load[q], q))
+        owner[k] = r
+        load[r] += items[k][2] ** 2
+    return [k for k in range(len(items)) if owner[k] == rank]
 
 
 def batch_specs(count: int = 256, seed: int = BATCH_SEED, n_lo: int = 128, n_hi: int = 4096,
