@@ -22,8 +22,8 @@
 //   FP64, strict   every point in the reference order with binary64 instructions (bit-exact)
 //   FP64, exact    power-of-two stencils on a certified tile: integer evaluation with identical
 //                  bits (prk_fixed.cuh), falling back to strict per tile
-//   FP32C          paired antisymmetric differences from register row segments, split weights,
-//                  TwoSum, two-float out (prk_arith.cuh)
+//   FP32C          paired antisymmetric differences from register row segments, summed per weight
+//                  group, split weights, TwoSum, two-float out (prk_arith.cuh)
 #pragma once
 
 #include <cuda.h>
@@ -136,34 +136,68 @@ __device__ __forceinline__ void ld_seg_i(const int64_t* p, I (&v)[N])
 // ---------------------------------------------------------------------------------------------
 // FP32C: the stencil sums of CPT points of one row. s points at in(r, c0) in the smem tile.
 
+// The taps of a PRK stencil share few distinct weights: star R has R (1/(2kR) on the k-th ring of
+// the cross), grid R has 2R (the sides and the diagonal of each ring). Group g collects the paired
+// differences whose weight is +-c_g: D_g = sum of sign * (in[p+d] - in[p-d]). Every tap's two values
+// are read and differenced; the sums within a group are exact for integer fields (they stay below
+// 2^24), and the weights then enter through NG compensated products instead of one per tap.
+template <int P, int R>
+__host__ __device__ constexpr int group_count() { return P == STAR ? R : 2 * R; }
+
+// Group of the positive tap (dc, dr) (dr > 0, or dr == 0 and dc > 0) and the sign of its weight.
+template <int P, int R>
+__host__ __device__ constexpr int group_of(int dc, int dr)
+{
+    const int adc = dc > 0 ? dc : -dc, adr = dr > 0 ? dr : -dr;
+    const int m = adc > adr ? adc : adr;
+    if (P == STAR) return m - 1;
+    return (adc == m && adr == m) ? R + m - 1 : m - 1;  // diagonal of ring m, else its sides
+}
+
+// |weight| of group g, as a (hi, lo) float pair.
+template <int P, int R>
+__host__ __device__ constexpr double group_weight(int g)
+{
+    if (P == STAR) return weight(STAR, R, 0, g + 1);
+    return g < R ? weight(GRID, R, 0, g + 1) : weight(GRID, R, g - R + 1, g - R + 1);
+}
+
+// Every positive tap's |weight| is its group's weight (checked at compile time for all stencils).
+template <int P, int R>
+__host__ __device__ constexpr bool groups_ok()
+{
+    for (int dr = 0; dr <= R; ++dr)
+        for (int dc = -R; dc <= R; ++dc) {
+            if (dr == 0 && dc <= 0) continue;
+            const double w = weight(P, R, dc, dr);
+            if (w != 0.0 && (w > 0 ? w : -w) != group_weight<P, R>(group_of<P, R>(dc, dr))) return false;
+        }
+    return true;
+}
+static_assert(groups_ok<STAR, 1>() && groups_ok<STAR, 2>() && groups_ok<STAR, 3>() && groups_ok<STAR, 4>() &&
+                  groups_ok<STAR, 5>() && groups_ok<GRID, 1>() && groups_ok<GRID, 2>() && groups_ok<GRID, 3>() &&
+                  groups_ok<GRID, 4>() && groups_ok<GRID, 5>(),
+              "weight groups");
+
 template <int P, int R, int CPT, int RA>
 __device__ __forceinline__ void fp32c_points(const float* s, int ld, float (&sh)[CPT], float (&sl)[CPT])
 {
     constexpr int SEG = CPT + 2 * RA;
-    bool first = true;
-    auto acc = [&](int k, float w_hi, float w_lo, float d) {
-        const float p = __fmul_rn(w_hi, d);
-        float pe = __fmaf_rn(w_hi, d, -p);
-        pe = __fmaf_rn(w_lo, d, pe);
-        if (first) {
-            sh[k] = p;
-            sl[k] = pe;
-        } else {
-            float t, e;
-            two_sum(sh[k], p, t, e);
-            sh[k] = t;
-            sl[k] = __fadd_rn(sl[k], __fadd_rn(e, pe));
-        }
-    };
+    constexpr int NG = group_count<P, R>();
+    float D[NG][CPT];
+#pragma unroll
+    for (int g = 0; g < NG; ++g)
+#pragma unroll
+        for (int k = 0; k < CPT; ++k) D[g][k] = 0.0f;
     {
         float m0[SEG];
         ld_seg<SEG>(s - RA, m0);
 #pragma unroll
         for (int dc = 1; dc <= R; ++dc) {
-            const double w = weight(P, R, dc, 0);
+            constexpr int dr = 0;
+            const int g = group_of<P, R>(dc, dr);
 #pragma unroll
-            for (int k = 0; k < CPT; ++k) acc(k, split_hi(w), split_lo(w), __fsub_rn(m0[k + RA + dc], m0[k + RA - dc]));
-            first = false;
+            for (int k = 0; k < CPT; ++k) D[g][k] = __fadd_rn(D[g][k], __fsub_rn(m0[k + RA + dc], m0[k + RA - dc]));
         }
     }
 #pragma unroll
@@ -172,21 +206,46 @@ __device__ __forceinline__ void fp32c_points(const float* s, int ld, float (&sh)
             float up[CPT], dn[CPT];
             ld_seg<CPT>(s + dr * ld, up);
             ld_seg<CPT>(s - dr * ld, dn);
-            const double w = weight(P, R, 0, dr);
+            const int g = group_of<P, R>(0, dr);
 #pragma unroll
-            for (int k = 0; k < CPT; ++k) acc(k, split_hi(w), split_lo(w), __fsub_rn(up[k], dn[k]));
+            for (int k = 0; k < CPT; ++k) D[g][k] = __fadd_rn(D[g][k], __fsub_rn(up[k], dn[k]));
         } else {
             float up[SEG], dn[SEG];
             ld_seg<SEG>(s + dr * ld - RA, up);
             ld_seg<SEG>(s - dr * ld - RA, dn);
 #pragma unroll
             for (int dc = -R; dc <= R; ++dc) {
-                const double w = weight(P, R, dc, dr);
-                if (w != 0.0) {
+                const int sg = weight_sign(P, R, dc, dr);
+                if (sg != 0) {
+                    const int g = group_of<P, R>(dc, dr);
 #pragma unroll
-                    for (int k = 0; k < CPT; ++k)
-                        acc(k, split_hi(w), split_lo(w), __fsub_rn(up[k + RA + dc], dn[k + RA - dc]));
+                    for (int k = 0; k < CPT; ++k) {
+                        const float d = __fsub_rn(up[k + RA + dc], dn[k + RA - dc]);
+                        D[g][k] = sg > 0 ? __fadd_rn(D[g][k], d) : __fsub_rn(D[g][k], d);
+                    }
                 }
+            }
+        }
+    }
+    // S = sum over groups of c_g * D_g: products with split weights and their errors through FMA,
+    // the sum through TwoSum, giving (hi, lo)
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+        const double w = group_weight<P, R>(g);
+        const float wh = split_hi(w), wl = split_lo(w);
+#pragma unroll
+        for (int k = 0; k < CPT; ++k) {
+            const float p = __fmul_rn(wh, D[g][k]);
+            float pe = __fmaf_rn(wh, D[g][k], -p);
+            pe = __fmaf_rn(wl, D[g][k], pe);
+            if (g == 0) {
+                sh[k] = p;
+                sl[k] = pe;
+            } else {
+                float t, e;
+                two_sum(sh[k], p, t, e);
+                sh[k] = t;
+                sl[k] = __fadd_rn(sl[k], __fadd_rn(e, pe));
             }
         }
     }
@@ -619,6 +678,7 @@ template <int P, int R, int DT, int STEPS, int TH_>
 constexpr int min_blocks()
 {
     if (DT == FP64 && !pow2_weights(P, R)) return STEPS == 1 ? 2 : 1;
+    if (DT == FP32C && P == GRID && R >= 3) return 2;  // bound by FP32 issue: registers over residency
     const int b = Geo<DT, R, TH_>::CTAS;
     return STEPS == 1 ? b : (b < 3 ? b : 3);
 }
