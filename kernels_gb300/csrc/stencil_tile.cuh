@@ -502,6 +502,9 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
         __syncthreads();  // every converted word visible
     }
 
+    // Set by the multi-application FP32 route when the warp's out words are held as integers
+    bool oint = false;
+
     // S of CPT points of row r (tile coordinates) added into the out words o[] (in place)
     auto apply_row = [&](int r, uint64_t* o) {
         const int soff = (r + R) * G::SW + G::RA + c0;  // in(r, c0) in the tile
@@ -513,8 +516,13 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
                 if (fexact) {
                     float S[CPT];
                     fexact_points<P, R, CPT, G::RA>(reinterpret_cast<const float*>(s_in) + soff, G::SW, S);
+                    if (oint) {
 #pragma unroll
-                    for (int k = 0; k < CPT; ++k) o[k] = as_bits(__dadd_rn(as_dbl(o[k]), as_dbl(f2d(S[k], -SHIFT))));
+                        for (int k = 0; k < CPT; ++k) o[k] += static_cast<uint64_t>(static_cast<int64_t>(__float2int_rn(S[k])));
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < CPT; ++k) o[k] = as_bits(__dadd_rn(as_dbl(o[k]), as_dbl(f2d(S[k], -SHIFT))));
+                    }
                     done = true;
                 } else if (unit != fx::NOT_FIXED) {
                     if (narrow) {
@@ -634,6 +642,37 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
 #pragma unroll
             for (int k = 0; k < CPT; ++k) o[rr][k] = row_out ? load_out(r, k) : 0ull;
         }
+        if constexpr (EXACT) {
+            // FP32 route: when every out word the warp stores is an integer V of 2^-SHIFT units with
+            // |V| < 2^30, out is held as V. Every S is an integer below 2^24 units, so each binary64
+            // add of the reference chain (out + S) is exact, the running V stays below 2^31 and its
+            // conversion at the end gives the same bits; a zero comes out +0 both ways (S is never
+            // -0). The applications then add integers instead of issuing binary64 adds.
+            if (fexact) {
+                constexpr int SHIFT = pow2_shift(P, R);
+                bool ok = true;
+#pragma unroll
+                for (int rr = 0; rr < ROWS; ++rr) {
+                    const int64_t gi = i0 + warp + WARPS * rr;
+                    const bool row_out = col_ok && gi < n && has_out && gi >= R && gi < n - R;
+#pragma unroll
+                    for (int k = 0; k < CPT; ++k) {
+                        int lo, hi;
+                        fx::classify(o[rr][k], lo, hi);
+                        const bool stored = row_out && gj + k >= R && gj + k < n - R;
+                        const bool fits = (o[rr][k] << 1) == 0 || (lo >= -SHIFT && hi <= 29 - SHIFT);
+                        ok = ok && (!stored || fits);
+                    }
+                }
+                oint = __all_sync(0xffffffffu, ok);
+                if (oint) {
+#pragma unroll
+                    for (int rr = 0; rr < ROWS; ++rr)
+#pragma unroll
+                        for (int k = 0; k < CPT; ++k) o[rr][k] = static_cast<uint64_t>(fx::to_fixed(o[rr][k], -SHIFT));
+                }
+            }
+        }
 #pragma unroll 1
         for (int t = 0; t < STEPS; ++t) {
             if (t > 0) {  // advance the whole tile, halo included: in_{k+1} = in_k + 1
@@ -659,6 +698,13 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
                 if (!col_ok || gi >= n || !(has_out && gi >= R && gi < n - R)) continue;
                 apply_row(r, o[rr]);
             }
+        }
+        if (oint) {
+#pragma unroll
+            for (int rr = 0; rr < ROWS; ++rr)
+#pragma unroll
+                for (int k = 0; k < CPT; ++k)
+                    o[rr][k] = from_fixed32(static_cast<int32_t>(o[rr][k]), -pow2_shift(P, R));
         }
 #pragma unroll
         for (int rr = 0; rr < ROWS; ++rr) {
