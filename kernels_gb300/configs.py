@@ -1,7 +1,8 @@
 """Run the stencil's measurement configurations beyond the headline one and print one JSON line per
 case. The cases are seeded synthetic PRK fields (in = i+j, out = 0), the same shapes as:
 
-  sweep   star and grid, R = 1..5, n = 32768, 50 iterations, FP64 and FP32C (tuned depth each):
+  sweep   star and grid, R = 1..5, n = 32768, 50 iterations, FP64 and FP32C (tuned depth each, or
+          the TMA kernel at --depth D without tuning):
           PRK GFLOP/s, algorithmic HBM GB/s and its fraction of the measured peak, the norm check,
           and the FP32C relative error against the FP64 result (bit-identical to the reference's)
   large   star R=4, FP32C at n = 65536 and FP64 at n = 46000, 200 iterations, tuned depth
@@ -41,13 +42,20 @@ def sample_points(n: int, r: int, count: int = 256, seed: int = 9):
     return [(int(i), int(j)) for i, j in rng.integers(r, n - r, (count, 2))]
 
 
-def one_case(torch, pattern: int, r: int, n: int, iterations: int, dtype: int, pts):
-    """A PRK run with the tuned kernel and depth; returns (record, sampled out values)."""
+def one_case(torch, pattern: int, r: int, n: int, iterations: int, dtype: int, pts, depth: int | None = None):
+    """A PRK run with the tuned kernel and depth (or the TMA kernel at a fixed depth, untuned);
+    returns (record, sampled out values)."""
     in_a, in_b, out = kg.alloc(n, dtype)
     kg.init(in_a, out)
-    tuning = kg.tune(pattern, r, n, dtype)
+    if depth is None:
+        tuning = kg.tune(pattern, r, n, dtype)
+    else:
+        tuning = {"depth": depth, "kernel": "fixed", "tile_rows": 32, "tile_cols": 0, "cols_per_thread": 0}
     t0 = time.perf_counter()
-    res = kg.run(pattern, r, iterations, in_a, in_b, out, tuned=True)
+    if depth is None:
+        res = kg.run(pattern, r, iterations, in_a, in_b, out, tuned=True)
+    else:
+        res = kg.run(pattern, r, iterations, in_a, in_b, out, depth=depth)
     wall = time.perf_counter() - t0
     nrm = kg.norm(r, out)
     idx = torch.tensor([i * n + j for i, j in pts], device="cuda")
@@ -71,12 +79,12 @@ def one_case(torch, pattern: int, r: int, n: int, iterations: int, dtype: int, p
     return rec, vals
 
 
-def run_pair(torch, pattern, r, n64, n32, iterations):
+def run_pair(torch, pattern, r, n64, n32, iterations, depth=None):
     pts64 = sample_points(n64, r)
-    rec64, v64 = one_case(torch, pattern, r, n64, iterations, kg.FP64, pts64)
+    rec64, v64 = one_case(torch, pattern, r, n64, iterations, kg.FP64, pts64, depth)
     print(json.dumps(rec64), flush=True)
     pts32 = sample_points(n32, r)
-    rec32, v32 = one_case(torch, pattern, r, n32, iterations, kg.FP32C, pts32)
+    rec32, v32 = one_case(torch, pattern, r, n32, iterations, kg.FP32C, pts32, depth)
     if n32 == n64:
         rec32["rel_err_vs_fp64"] = float(np.max(np.abs(v32 - v64) / np.abs(v64)))
     else:
@@ -128,7 +136,7 @@ def main() -> None:
         k = args.iterations or 50
         for name in args.patterns.split(","):
             for r in (int(x) for x in args.radii.split(",")):
-                run_pair(torch, kg.pattern_of(name), r, n, n, k)
+                run_pair(torch, kg.pattern_of(name), r, n, n, k, args.depth)
     elif args.which == "large":
         k = args.iterations or 200
         run_pair(torch, kg.STAR, 4, args.n or 46000, 65536, k)

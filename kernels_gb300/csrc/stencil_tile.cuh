@@ -389,6 +389,59 @@ __device__ __forceinline__ uint64_t from_fixed_any(int32_t x, int unit) { return
 __device__ __forceinline__ double as_dbl(uint64_t b) { return __longlong_as_double(static_cast<long long>(b)); }
 __device__ __forceinline__ uint64_t as_bits(double d) { return static_cast<uint64_t>(__double_as_longlong(d)); }
 
+// in += 1 over the whole staged tile, halo included, as 16-byte vectors (the tile starts at the
+// 128-byte aligned stage and its element count is a multiple of four): FP32 values (the FP32 route
+// and FP32C), integers in fixed-point units (one = 1.0 in those units) or binary64 values.
+template <int ELEMS>
+__device__ __forceinline__ void advance_f32(float* p)
+{
+    constexpr int NV = ELEMS / 4;
+#pragma unroll
+    for (int q = 0; q < (NV + THREADS - 1) / THREADS; ++q) {
+        const int idx = threadIdx.x + q * THREADS;
+        if (NV % THREADS == 0 || idx < NV) {
+            float4 v = reinterpret_cast<float4*>(p)[idx];
+            v.x = __fadd_rn(v.x, 1.0f);
+            v.y = __fadd_rn(v.y, 1.0f);
+            v.z = __fadd_rn(v.z, 1.0f);
+            v.w = __fadd_rn(v.w, 1.0f);
+            reinterpret_cast<float4*>(p)[idx] = v;
+        }
+    }
+}
+
+template <int ELEMS>
+__device__ __forceinline__ void advance_i64(int64_t* p, int64_t one)
+{
+    constexpr int NV = ELEMS / 2;
+#pragma unroll
+    for (int q = 0; q < (NV + THREADS - 1) / THREADS; ++q) {
+        const int idx = threadIdx.x + q * THREADS;
+        if (NV % THREADS == 0 || idx < NV) {
+            longlong2 v = reinterpret_cast<longlong2*>(p)[idx];
+            v.x += one;
+            v.y += one;
+            reinterpret_cast<longlong2*>(p)[idx] = v;
+        }
+    }
+}
+
+template <int ELEMS>
+__device__ __forceinline__ void advance_f64(double* p)
+{
+    constexpr int NV = ELEMS / 2;
+#pragma unroll
+    for (int q = 0; q < (NV + THREADS - 1) / THREADS; ++q) {
+        const int idx = threadIdx.x + q * THREADS;
+        if (NV % THREADS == 0 || idx < NV) {
+            double2 v = reinterpret_cast<double2*>(p)[idx];
+            v.x = __dadd_rn(v.x, 1.0);
+            v.y = __dadd_rn(v.y, 1.0);
+            reinterpret_cast<double2*>(p)[idx] = v;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------------------------
 // The kernel
 
@@ -518,7 +571,8 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
                     fexact_points<P, R, CPT, G::RA>(reinterpret_cast<const float*>(s_in) + soff, G::SW, S);
                     if (oint) {
 #pragma unroll
-                        for (int k = 0; k < CPT; ++k) o[k] += static_cast<uint64_t>(static_cast<int64_t>(__float2int_rn(S[k])));
+                        for (int k = 0; k < CPT; ++k)
+                            o[k] = static_cast<uint32_t>(static_cast<uint32_t>(o[k]) + static_cast<uint32_t>(__float2int_rn(S[k])));
                     } else {
 #pragma unroll
                         for (int k = 0; k < CPT; ++k) o[k] = as_bits(__dadd_rn(as_dbl(o[k]), as_dbl(f2d(S[k], -SHIFT))));
@@ -633,14 +687,16 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
         }
     } else {
         // out of the thread's points stays in registers across the applications
+        static_assert(G::ELEMS % 4 == 0, "the in-place advance moves 16-byte vectors");
         uint64_t o[ROWS][CPT];
+        bool ract[ROWS];  // the row holds interior points
 #pragma unroll
         for (int rr = 0; rr < ROWS; ++rr) {
             const int r = warp + WARPS * rr;
             const int64_t gi = i0 + r;
-            const bool row_out = col_ok && gi < n && has_out && gi >= R && gi < n - R;
+            ract[rr] = col_ok && gi < n && has_out && gi >= R && gi < n - R;
 #pragma unroll
-            for (int k = 0; k < CPT; ++k) o[rr][k] = row_out ? load_out(r, k) : 0ull;
+            for (int k = 0; k < CPT; ++k) o[rr][k] = ract[rr] ? load_out(r, k) : 0ull;
         }
         if constexpr (EXACT) {
             // FP32 route: when every out word the warp stores is an integer V of 2^-SHIFT units with
@@ -653,13 +709,11 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
                 bool ok = true;
 #pragma unroll
                 for (int rr = 0; rr < ROWS; ++rr) {
-                    const int64_t gi = i0 + warp + WARPS * rr;
-                    const bool row_out = col_ok && gi < n && has_out && gi >= R && gi < n - R;
 #pragma unroll
                     for (int k = 0; k < CPT; ++k) {
                         int lo, hi;
                         fx::classify(o[rr][k], lo, hi);
-                        const bool stored = row_out && gj + k >= R && gj + k < n - R;
+                        const bool stored = ract[rr] && gj + k >= R && gj + k < n - R;
                         const bool fits = (o[rr][k] << 1) == 0 || (lo >= -SHIFT && hi <= 29 - SHIFT);
                         ok = ok && (!stored || fits);
                     }
@@ -669,7 +723,8 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
 #pragma unroll
                     for (int rr = 0; rr < ROWS; ++rr)
 #pragma unroll
-                        for (int k = 0; k < CPT; ++k) o[rr][k] = static_cast<uint64_t>(fx::to_fixed(o[rr][k], -SHIFT));
+                        for (int k = 0; k < CPT; ++k)  // V in the low word (|V| < 2^31), high word zero
+                            o[rr][k] = static_cast<uint32_t>(static_cast<int32_t>(fx::to_fixed(o[rr][k], -SHIFT)));
                 }
             }
         }
@@ -677,34 +732,33 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
         for (int t = 0; t < STEPS; ++t) {
             if (t > 0) {  // advance the whole tile, halo included: in_{k+1} = in_k + 1
                 __syncthreads();
-                for (int idx = threadIdx.x; idx < G::ELEMS; idx += THREADS) {
-                    if constexpr (DT == FP64) {
-                        if (EXACT && fexact)
-                            reinterpret_cast<float*>(s_in)[idx] = __fadd_rn(reinterpret_cast<float*>(s_in)[idx], 1.0f);
-                        else if (EXACT && unit != fx::NOT_FIXED)
-                            reinterpret_cast<int64_t*>(s_in)[idx] += (1ll << (-unit));
-                        else
-                            s_in[idx] = __dadd_rn(s_in[idx], 1.0);
-                    } else {
-                        s_in[idx] = __fadd_rn(s_in[idx], 1.0f);
+                if constexpr (DT == FP64) {
+                    bool adv = false;
+                    if constexpr (EXACT) {
+                        if (fexact) {
+                            advance_f32<G::ELEMS>(reinterpret_cast<float*>(s_in));
+                            adv = true;
+                        } else if (unit != fx::NOT_FIXED) {
+                            advance_i64<G::ELEMS>(reinterpret_cast<int64_t*>(s_in), 1ll << (-unit));
+                            adv = true;
+                        }
                     }
+                    if (!adv) advance_f64<G::ELEMS>(s_in);
+                } else {
+                    advance_f32<G::ELEMS>(s_in);
                 }
                 __syncthreads();
             }
 #pragma unroll
-            for (int rr = 0; rr < ROWS; ++rr) {
-                const int r = warp + WARPS * rr;
-                const int64_t gi = i0 + r;
-                if (!col_ok || gi >= n || !(has_out && gi >= R && gi < n - R)) continue;
-                apply_row(r, o[rr]);
-            }
+            for (int rr = 0; rr < ROWS; ++rr)
+                if (ract[rr]) apply_row(warp + WARPS * rr, o[rr]);
         }
         if (oint) {
 #pragma unroll
             for (int rr = 0; rr < ROWS; ++rr)
 #pragma unroll
                 for (int k = 0; k < CPT; ++k)
-                    o[rr][k] = from_fixed32(static_cast<int32_t>(o[rr][k]), -pow2_shift(P, R));
+                    o[rr][k] = from_fixed32(static_cast<int32_t>(static_cast<uint32_t>(o[rr][k])), -pow2_shift(P, R));
         }
 #pragma unroll
         for (int rr = 0; rr < ROWS; ++rr) {
