@@ -57,6 +57,11 @@ extern "C" {
 #define PRK_RUN_DEPTH(d) ((d) << 8)
 /* Tall tiles: 64 rows per TMA tile (8 rows per thread) instead of 32 (4 per thread). */
 #define PRK_RUN_TALL 8
+/* All timed applications in one launch: every tile carries iterations 1..K in shared memory (in
+ * evolves pointwise, so a tile needs only its own rows and the R-row halo of the initial in). The
+ * results are those of K single applications. Needs the TMA shape (as prk_gb300_stencil_steps);
+ * overrides PRK_RUN_DEPTH and the tuned depth. */
+#define PRK_RUN_WHOLE 16
 
 /* One application of the stencil (replaces starR/gridR, stencil_openmp.hpp:1, stencil_cuda.hpp:1):
  *   out[i*n+j] += sum over taps of w * in[(i+dr)*n + (j+dc)]   for R <= i,j < n-R,
@@ -99,12 +104,16 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
                   int flags, double* elapsed_s, int* final_in, void* stream);
 
 /* A whole PRK run from host memory, the way Cxx11/stencil-cuda.cu drives it (:193-226): copies
- * h_in and h_out to the device, runs iterations+1 fused applications with the autotuner's kernel and
- * temporal depth (PRK_RUN_TUNED), copies out (and the final in, when h_in_final != NULL) back, and
- * computes the norm. Its device buffers are allocated on first use and kept for later calls (grown
- * when a larger grid comes); prk_gb300_release frees them. Calls are serialised process-wide.
+ * h_in and h_out to the device, runs iterations+1 fused applications, copies out (and the final in,
+ * when h_in_final != NULL) back, and computes the norm. For the TMA shape (n a multiple of 2 for
+ * PRK_FP64, 4 for PRK_FP32C) the grid goes in bands of rows: each band's copies in, its one launch
+ * carrying all iterations+1 applications, and its copies back overlap those of the other bands.
+ * Other shapes copy in, run with the autotuner's choice (PRK_RUN_TUNED) and copy back. Its device
+ * buffers and streams are allocated on first use and kept for later calls (the buffers grown when
+ * a larger grid comes); prk_gb300_release frees them. Calls are serialised process-wide.
  * *elapsed_s (optional) is the whole call's wall time including the copies; *kernel_s (optional)
- * the event time of iterations 1..K. Host buffers may be pageable or pinned. */
+ * the event time of the evaluation: the span of the band launches, or iterations 1..K. Host
+ * buffers may be pageable or pinned (pinned ones let the copies overlap). */
 int prk_gb300_run_host(int pattern, int radius, int64_t n, int dtype, int iterations, const void* h_in, void* h_out,
                        void* h_in_final, double* norm, double* elapsed_s, double* kernel_s);
 

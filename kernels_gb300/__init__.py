@@ -29,7 +29,7 @@ from ._lib import PrkError, check, load
 
 STAR, GRID = 0, 1
 FP64, FP32C = 0, 1
-RUN_GRAPH, RUN_UNFUSED, RUN_TUNED, RUN_TALL = 1, 2, 4, 8
+RUN_GRAPH, RUN_UNFUSED, RUN_TUNED, RUN_TALL, RUN_WHOLE = 1, 2, 4, 8, 16
 
 __all__ = ["STAR", "GRID", "FP64", "FP32C", "PrkError", "apply", "add", "init", "norm", "run", "run_host",
            "alloc", "apply_steps", "flops", "tune", "Batch", "pattern_of", "dtype_of", "version", "set_kernel", "status", "KERNEL_AUTO",
@@ -162,14 +162,14 @@ class RunResult:
 
 
 def run(pattern: int, radius: int, iterations: int, in_a, in_b, out, graph: bool = False, unfused: bool = False,
-        stream=None, depth: int = 1, tuned: bool = False, tall: bool = False) -> RunResult:
+        stream=None, depth: int = 1, tuned: bool = False, tall: bool = False, whole: bool = False) -> RunResult:
     n = _n_of(in_a)
     dt = dtype_of(in_a)
     _check_out(out, n, dt)
     el = C.c_double()
     fin = C.c_int()
     flags = (RUN_GRAPH if graph else 0) | (RUN_UNFUSED if unfused else 0) | (depth << 8) | (RUN_TUNED if tuned else 0) \
-        | (RUN_TALL if tall else 0)
+        | (RUN_TALL if tall else 0) | (RUN_WHOLE if whole else 0)
     check(load().prk_gb300_run(pattern, radius, n, dt, iterations, in_a.data_ptr(),
                                None if in_b is None else in_b.data_ptr(), out.data_ptr(), flags, C.byref(el),
                                C.byref(fin), _stream(stream)))

@@ -1,6 +1,7 @@
 // C ABI of libprk_gb300.so (declared in include/prk_gb300.h): argument checks, dispatch to the
 // kernel launchers, the timed iteration loop and the host-buffer entry point. Errors are returned,
 // never raised: a negative PRK_ERR_* for a rejected call, a positive cudaError_t otherwise.
+#include <algorithm>
 #include <chrono>
 #include <cstdarg>
 #include <cstdio>
@@ -103,11 +104,13 @@ int norm_scratch(double** out)
     return PRK_OK;
 }
 
-// Device buffers of prk_gb300_run_host, kept between calls (grown when a larger grid comes) and
-// freed by prk_gb300_release.
+// Device buffers and streams of prk_gb300_run_host, kept between calls (the buffers grown when a
+// larger grid comes) and freed by prk_gb300_release. Streams: copies in, copies out, and two for
+// the band launches.
 struct HostWorkspace {
     void* d[3] = {nullptr, nullptr, nullptr};
     int64_t in_bytes = 0, out_bytes = 0;
+    cudaStream_t s[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 std::mutex g_host_mu;
 std::vector<HostWorkspace> g_host_ws;
@@ -265,13 +268,15 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
     if (iterations < 1) return fail(PRK_ERR_ARG, "iterations must be >= 1");
     const bool unfused = (flags & PRK_RUN_UNFUSED) != 0;
     const bool graph = (flags & PRK_RUN_GRAPH) != 0;
+    const bool whole = (flags & PRK_RUN_WHOLE) != 0;
+    if (whole && unfused) return fail(PRK_ERR_ARG, "PRK_RUN_WHOLE is a fused form");
     int depth = (flags >> 8) & 0xFF;
     if (depth == 0) depth = 1;
     if (!prk::tma_depth_ok(depth)) return fail(PRK_ERR_ARG, "temporal depth %d is not 1, 2, 4 or 8", depth);
     if (!in_a || !out || (!unfused && !in_b)) return fail(PRK_ERR_ARG, "null buffer");
     bool tuned_generic = false;
     int rows = (flags & PRK_RUN_TALL) ? 64 : 32;
-    if ((flags & PRK_RUN_TUNED) && !unfused) {
+    if ((flags & PRK_RUN_TUNED) && !unfused && !whole) {
         prk_gb300_tuning t{};
         if (int rc = prk_gb300_tune(pattern, radius, n, dtype, 0, &t)) return rc;
         depth = t.depth;
@@ -319,8 +324,23 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
         }
         return PRK_OK;
     };
-    // `count` applications: launches of the temporal depth, the remainder in powers of two.
+    if (whole) {
+        prk::StencilCall probe{pattern, radius, n, dtype, in_a, in_b, out, nullptr};
+        if (g_kernel_choice == 1 || !prk::tma_eligible(probe))
+            return fail(PRK_ERR_ARG, "PRK_RUN_WHOLE needs the TMA tile kernels: 16-byte-aligned buffers, n a multiple of %d",
+                        dtype == PRK_FP64 ? 2 : 4);
+    }
+    // `count` applications: one launch (whole run), or launches of the temporal depth with the
+    // remainder in powers of two.
     auto steps = [&](cudaStream_t st, int count) -> int {
+        if (whole) {
+            DevScratch dsc;
+            if (int rc = dev_scratch(&dsc)) return rc;
+            prk::StencilCall c{pattern, radius, n, dtype, bufs[cur], bufs[cur ^ 1], out, st};
+            PRK_CUDA(prk::launch_stencil_tma_band(c, count, 0, n, dsc.status), "stencil launch (TMA tiles, whole run)");
+            cur ^= 1;
+            return PRK_OK;
+        }
         if (depth == 1) {
             for (int i = 0; i < count; ++i)
                 if (int rc = step(st)) return rc;
@@ -386,12 +406,111 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
     return rc;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Events of one banded run, destroyed on scope exit.
+struct BandEvents {
+    std::vector<cudaEvent_t> ev;
+    ~BandEvents()
+    {
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+    cudaError_t make(size_t count, unsigned flags)
+    {
+        ev.assign(count, nullptr);
+        for (cudaEvent_t& e : ev)
+            if (cudaError_t ce = cudaEventCreateWithFlags(&e, flags)) return ce;
+        return cudaSuccess;
+    }
+};
+
+// The host-buffer run in bands of rows. `in` evolves pointwise, so a band's `out` after every
+// application depends only on its own rows of `out` and its rows of `in` with R more on either
+// side, and one launch of the run-time-depth tile kernel carries all `apps` applications of the
+// band. The bands' copies to the device go in order on one stream; band b is launched once its
+// rows and the next band's (its lower halo) have landed, on one of two streams so that one band's
+// last wave overlaps the next band's first; its rows go back to the host as soon as it is done.
+// Copies in, evaluation and copies out of different bands overlap.
+int run_host_banded(HostWorkspace& ws, int pattern, int radius, int64_t n, int dtype, int apps, const void* h_in,
+                    void* h_out, void* h_in_final, double* norm, double* kernel_s)
+{
+    DevScratch sc;
+    if (int rc = dev_scratch(&sc)) return rc;
+    for (cudaStream_t& st : ws.s)
+        if (!st) PRK_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+    cudaStream_t s_in = ws.s[0], s_out = ws.s[1], s_ev[2] = {ws.s[2], ws.s[3]};
+    struct Drain {  // no copy of the caller's host buffers outlives the call, on any return
+        cudaStream_t* s;
+        ~Drain()
+        {
+            for (int i = 0; i < 4; ++i) cudaStreamSynchronize(s[i]);
+        }
+    } drain{ws.s};
+    const int64_t es = dtype == PRK_FP64 ? 8 : 4;  // bytes per `in` element; `out` has 8
+    const int64_t band = std::max<int64_t>(128, (n / 32 + 31) / 32 * 32);
+    const int nb = static_cast<int>((n + band - 1) / band);
+    BandEvents landed, done, span;
+    PRK_CUDA(landed.make(nb, cudaEventDisableTiming), "cudaEventCreate");
+    PRK_CUDA(done.make(nb, cudaEventDisableTiming), "cudaEventCreate");
+    PRK_CUDA(span.make(2, cudaEventDefault), "cudaEventCreate");
+    char* d_in = static_cast<char*>(ws.d[0]);
+    char* d_fin = static_cast<char*>(ws.d[1]);
+    char* d_out = static_cast<char*>(ws.d[2]);
+    const char* hi = static_cast<const char*>(h_in);
+    char* ho = static_cast<char*>(h_out);
+    char* hf = static_cast<char*>(h_in_final);
+    for (int b = 0; b < nb; ++b) {
+        const int64_t r0 = b * band, rows = std::min(band, n - r0);
+        PRK_CUDA(cudaMemcpyAsync(d_in + r0 * n * es, hi + r0 * n * es, rows * n * es, cudaMemcpyHostToDevice, s_in),
+                 "host to device copy");
+        PRK_CUDA(cudaMemcpyAsync(d_out + r0 * n * 8, ho + r0 * n * 8, rows * n * 8, cudaMemcpyHostToDevice, s_in),
+                 "host to device copy");
+        PRK_CUDA(cudaEventRecord(landed.ev[b], s_in), "cudaEventRecord");
+    }
+    for (int b = 0; b < nb; ++b) {
+        const int64_t r0 = b * band, rows = std::min(band, n - r0);
+        cudaStream_t st = s_ev[b & 1];
+        PRK_CUDA(cudaStreamWaitEvent(st, landed.ev[b + 1 < nb ? b + 1 : b], 0), "cudaStreamWaitEvent");
+        if (b == 0) PRK_CUDA(cudaEventRecord(span.ev[0], st), "cudaEventRecord");
+        prk::StencilCall c{pattern, radius, n, dtype, d_in, d_fin, d_out, st};
+        PRK_CUDA(prk::launch_stencil_tma_band(c, apps, r0, rows, sc.status), "band launch (TMA tiles)");
+        PRK_CUDA(cudaEventRecord(done.ev[b], st), "cudaEventRecord");
+        PRK_CUDA(cudaStreamWaitEvent(s_out, done.ev[b], 0), "cudaStreamWaitEvent");
+        PRK_CUDA(cudaMemcpyAsync(ho + r0 * n * 8, d_out + r0 * n * 8, rows * n * 8, cudaMemcpyDeviceToHost, s_out),
+                 "device to host copy");
+        if (hf)
+            PRK_CUDA(cudaMemcpyAsync(hf + r0 * n * es, d_fin + r0 * n * es, rows * n * es, cudaMemcpyDeviceToHost, s_out),
+                     "device to host copy");
+    }
+    // the norm after every band, on the first evaluation stream (the last two bands cover both)
+    if (nb > 1) PRK_CUDA(cudaStreamWaitEvent(s_ev[0], done.ev[nb - 2], 0), "cudaStreamWaitEvent");
+    PRK_CUDA(cudaStreamWaitEvent(s_ev[0], done.ev[nb - 1], 0), "cudaStreamWaitEvent");
+    PRK_CUDA(cudaEventRecord(span.ev[1], s_ev[0]), "cudaEventRecord");
+    if (norm) {
+        if (int rc = prk_gb300_norm(radius, n, dtype, d_out, norm, s_ev[0])) return rc;
+    }
+    PRK_CUDA(cudaStreamSynchronize(s_out), "copies back");
+    PRK_CUDA(cudaStreamSynchronize(s_ev[0]), "band evaluation");
+    PRK_CUDA(cudaStreamSynchronize(s_ev[1]), "band evaluation");
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, span.ev[0], span.ev[1]);
+    if (kernel_s) *kernel_s = ms * 1e-3;
+    return check_status();
+}
+
+}  // namespace
+
+extern "C" {
+
 int prk_gb300_run_host(int pattern, int radius, int64_t n, int dtype, int iterations, const void* h_in, void* h_out,
                        void* h_in_final, double* norm, double* elapsed_s, double* kernel_s)
 {
     const auto t0 = std::chrono::steady_clock::now();
     if (int rc = check_stencil(pattern, radius, n, dtype)) return rc;
-    if (iterations < 1) return fail(PRK_ERR_ARG, "iterations must be >= 1");
+    if (iterations < 1 || iterations > (1 << 30)) return fail(PRK_ERR_ARG, "iterations must be in 1..2^30");
     if (!h_in || !h_out) return fail(PRK_ERR_ARG, "h_in and h_out must be non-null");
     const int64_t ib = prk_gb300_bytes(n, dtype, 0), ob = prk_gb300_bytes(n, dtype, 1);
     int dev = 0;
@@ -423,6 +542,13 @@ int prk_gb300_run_host(int pattern, int radius, int64_t n, int dtype, int iterat
             ws.out_bytes = ob;
         }
         void** d = ws.d;
+        {
+            prk::StencilCall probe{pattern, radius, n, dtype, d[0], d[1], d[2], nullptr};
+            if (g_kernel_choice != 1 && prk::tma_eligible(probe)) {  // iteration 0 plus `iterations`
+                rc = run_host_banded(ws, pattern, radius, n, dtype, iterations + 1, h_in, h_out, h_in_final, norm, kernel_s);
+                break;
+            }
+        }
         if ((ce = cudaMemcpy(d[0], h_in, ib, cudaMemcpyHostToDevice)) != cudaSuccess ||
             (ce = cudaMemcpy(d[2], h_out, ob, cudaMemcpyHostToDevice)) != cudaSuccess) { rc = cuda_fail(ce, "host to device copy"); break; }
         int fin = 0;
@@ -446,6 +572,10 @@ int prk_gb300_release(void)
         for (void*& p : g_host_ws[dev].d) {
             if (p) cudaFree(p);
             p = nullptr;
+        }
+        for (cudaStream_t& st : g_host_ws[dev].s) {
+            if (st) cudaStreamDestroy(st);
+            st = nullptr;
         }
         g_host_ws[dev].in_bytes = g_host_ws[dev].out_bytes = 0;
     }

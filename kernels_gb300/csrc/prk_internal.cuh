@@ -37,6 +37,10 @@ bool tma_depth_ok(int steps);
 // Tile heights the TMA kernels are built for (32 and 64 rows).
 bool tma_rows_ok(int tile_rows);
 cudaError_t launch_stencil_tma(const StencilCall& c, int steps, unsigned* status, int tile_rows = 32);
+// All `depth` applications of a run in one launch over the tiles of grid rows [row0, row0 + rows)
+// (row0 a multiple of 32): reads `in` rows row0 - R .. row0 + rows + R - 1 and the band's `out`
+// rows, writes the band's in_next (in after `depth` updates) and out rows.
+cudaError_t launch_stencil_tma_band(const StencilCall& c, int depth, int64_t row0, int64_t rows, unsigned* status);
 
 // kernels_generic.cu: any n, any 8-byte-aligned pointers.
 cudaError_t launch_stencil_generic(const StencilCall& c);

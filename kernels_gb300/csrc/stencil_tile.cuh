@@ -16,7 +16,9 @@
 // shared memory, halo included, is advanced in place with the same rounded +1 the reference
 // applies, and the halo never grows. Every application reads the current `in` values and applies
 // every tap. `out` stays in registers and is rounded after each application as the reference
-// rounds it. HBM traffic per application drops by STEPS.
+// rounds it. HBM traffic per application drops by STEPS. STEPS = 0 takes the depth at run time
+// (`depth`, any count): a whole run in one launch per tile, as the host-buffer path uses it on
+// bands of rows.
 //
 // Evaluation modes:
 //   FP64, strict   every point in the reference order with binary64 instructions (bit-exact)
@@ -55,6 +57,8 @@ struct Cfg<FP32C, TH_> {
 };
 constexpr int TH_DEFAULT = 32;
 constexpr int TH_TALL = 64;
+// Deepest run-time depth for which the FP32 route holds: 15 * (2^20 + 65536) < 2^24.
+constexpr int FP32_MAX_STEPS = 65536;
 
 constexpr int SMEM_PER_SM = 228 * 1024;
 constexpr int SMEM_PER_CTA_MAX = 227 * 1024;
@@ -91,6 +95,9 @@ struct Launch {
     void* out;
     unsigned* status;
     cudaStream_t stream;
+    int depth;     // applications per launch for the run-time-depth kernels (STEPS = 0)
+    int64_t row0;  // first grid row of the launch's tiles (a multiple of the tile height)
+    int64_t rows;  // grid rows covered from row0 (0: to the end of the grid)
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -383,6 +390,23 @@ __device__ __forceinline__ uint64_t from_fixed32(int32_t x, int unit)
     return s | ((static_cast<uint64_t>(msb + unit + 1022) << 52) + m);
 }
 
+// out = V * 2^-shift for an integer V with |V| < 2^21, read from the binary64 encoding (+-0 give 0);
+// false for any other value. With M the 53-bit significand, V = M >> (k + 32) for
+// k = 1043 - shift - (biased exponent), an integer below 2^21 exactly when 0 <= k <= 20 and the
+// k + 32 bits shifted out are zero. Subnormals, infinities and NaNs fall outside that range of k.
+__device__ __forceinline__ bool out_units(uint64_t b, int shift, int32_t& V)
+{
+    const uint32_t hi = static_cast<uint32_t>(b >> 32), lo = static_cast<uint32_t>(b);
+    const uint32_t mag = hi & 0x7FFFFFFFu;
+    const int k = 1043 - shift - static_cast<int>(mag >> 20);
+    const uint32_t m = (mag & 0xFFFFFu) | 0x100000u;
+    const bool zero = (mag | lo) == 0u;
+    const bool ok = zero || (lo == 0u && k >= 0 && k <= 20 && (m & ((1u << (k & 31)) - 1u)) == 0u);
+    const int32_t a = static_cast<int32_t>(m >> (k & 31));
+    V = zero ? 0 : ((hi >> 31) ? -a : a);
+    return ok;
+}
+
 __device__ __forceinline__ uint64_t from_fixed_any(int64_t x, int unit) { return fx::from_fixed(x, unit); }
 __device__ __forceinline__ uint64_t from_fixed_any(int32_t x, int unit) { return from_fixed32(x, unit); }
 
@@ -451,15 +475,17 @@ __device__ __forceinline__ bool tile_has_out(int64_t i0, int64_t j0, int64_t n, 
     return (i0 + th > R) && (i0 < n - R) && (j0 + tw > R) && (j0 < n - R);
 }
 
-// Evaluate one tile whose `in` (with halo) is in shared memory: STEPS applications, then in_next
-// and out to HBM. GLOBAL_OUT = false: the out tile was loaded into shared memory next to `in` (TMA
-// path); true: out is read from HBM here (batched path). vec_ok: rows are 16-byte aligned and n is a
-// multiple of CPT, so a thread's CPT points move as one vector; otherwise they move one by one.
+// Evaluate one tile whose `in` (with halo) is in shared memory: STEPS applications (`depth` when
+// STEPS = 0), then in_next and out to HBM. GLOBAL_OUT = false: the out tile was loaded into shared
+// memory next to `in` (TMA path); true: out is read from HBM here (batched path). vec_ok: rows are
+// 16-byte aligned and n is a multiple of CPT, so a thread's CPT points move as one vector;
+// otherwise they move one by one.
 template <int P, int R, int DT, int STEPS, bool GLOBAL_OUT = false, int TH_ = 32>
 __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, int64_t i0, int64_t j0, int64_t n,
                                              bool has_out, void* __restrict__ in_next_v, void* __restrict__ out_v,
-                                             bool vec_ok = true)
+                                             bool vec_ok = true, int depth = 0)
 {
+    const int nsteps = STEPS > 0 ? STEPS : depth;
     using G = Geo<DT, R, TH_>;
     using C = Cfg<DT, TH_>;
     using T = typename C::T;
@@ -494,7 +520,8 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
         constexpr int SHIFT = pow2_shift(P, R);
         constexpr long long L1 = pow2_coef_l1(P, R);
         constexpr int PER = (G::ELEMS + THREADS - 1) / THREADS;
-        static_assert(L1 < 16 && STEPS <= 8, "FP32 route bound: (L1/2) * 2 * (2^20 + 8) < 2^24");
+        // FP32 route bound: L1 * (2^20 + steps) < 2^24 for L1 <= 15 and steps <= FP32_MAX_STEPS
+        static_assert(L1 < 16 && STEPS <= FP32_MAX_STEPS, "FP32 route bound");
         const uint64_t* raw = reinterpret_cast<const uint64_t*>(s_in);
         float fv[PER];
         bool ok = true;
@@ -510,6 +537,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
             ok = ok && (b == 0ull || (small && fr == f));
             fv[q] = b == 0ull ? 0.0f : f;
         }
+        if (STEPS == 0 && nsteps > FP32_MAX_STEPS) ok = false;
         ok = __syncthreads_and(ok) != 0;
         if (ok) {
             float* sf = reinterpret_cast<float*>(s_in);
@@ -541,12 +569,12 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
                 lo = min(lo, s_red[2 * w]);
                 hi = max(hi, s_red[2 * w + 1]);
             }
-            unit = fx::certify(lo, hi, SHIFT, L1, STEPS);
+            unit = fx::certify(lo, hi, SHIFT, L1, nsteps);
             if (unit != fx::NOT_FIXED) {
                 // int32 arithmetic suffices when every partial sum and every updated value stays below 2^31
                 const int span = hi == fx::ZERO_HI ? 0 : hi + 1 - unit;
                 narrow = span <= 30 && -unit <= 26 &&
-                         ((1ll << span) + static_cast<long long>(STEPS) * (1ll << (-unit))) < (1ll << 31) / L1;
+                         ((1ll << span) + static_cast<long long>(nsteps) * (1ll << (-unit))) < (1ll << 31) / L1;
                 __syncthreads();  // every thread has read its raw words
                 int64_t* iv = reinterpret_cast<int64_t*>(s_in);
                 for (int idx = threadIdx.x; idx < G::ELEMS; idx += THREADS) iv[idx] = fx::to_fixed(raw[idx], unit);
@@ -571,8 +599,12 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
                     fexact_points<P, R, CPT, G::RA>(reinterpret_cast<const float*>(s_in) + soff, G::SW, S);
                     if (oint) {
 #pragma unroll
-                        for (int k = 0; k < CPT; ++k)
-                            o[k] = static_cast<uint32_t>(static_cast<uint32_t>(o[k]) + static_cast<uint32_t>(__float2int_rn(S[k])));
+                        for (int k = 0; k < CPT; ++k) {
+                            if constexpr (STEPS == 0)
+                                o[k] += static_cast<uint64_t>(static_cast<int64_t>(__float2int_rn(S[k])));
+                            else
+                                o[k] = static_cast<uint32_t>(static_cast<uint32_t>(o[k]) + static_cast<uint32_t>(__float2int_rn(S[k])));
+                        }
                     } else {
 #pragma unroll
                         for (int k = 0; k < CPT; ++k) o[k] = as_bits(__dadd_rn(as_dbl(o[k]), as_dbl(f2d(S[k], -SHIFT))));
@@ -700,21 +732,21 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
         }
         if constexpr (EXACT) {
             // FP32 route: when every out word the warp stores is an integer V of 2^-SHIFT units with
-            // |V| < 2^30, out is held as V. Every S is an integer below 2^24 units, so each binary64
-            // add of the reference chain (out + S) is exact, the running V stays below 2^31 and its
-            // conversion at the end gives the same bits; a zero comes out +0 both ways (S is never
-            // -0). The applications then add integers instead of issuing binary64 adds.
+            // |V| < 2^21, out is held as V. Every S is an integer below 2^24 units, so each binary64
+            // add of the reference chain (out + S) is exact (the running V stays below 2^28 for 8
+            // applications, int32, and below 2^41 for FP32_MAX_STEPS, int64) and its conversion at
+            // the end gives the same bits; a zero comes out +0 both ways (S is never -0). The
+            // applications then add integers instead of issuing binary64 adds.
             if (fexact) {
                 constexpr int SHIFT = pow2_shift(P, R);
+                int32_t V[ROWS][CPT];
                 bool ok = true;
 #pragma unroll
                 for (int rr = 0; rr < ROWS; ++rr) {
 #pragma unroll
                     for (int k = 0; k < CPT; ++k) {
-                        int lo, hi;
-                        fx::classify(o[rr][k], lo, hi);
+                        const bool fits = out_units(o[rr][k], SHIFT, V[rr][k]);
                         const bool stored = ract[rr] && gj + k >= R && gj + k < n - R;
-                        const bool fits = (o[rr][k] << 1) == 0 || (lo >= -SHIFT && hi <= 29 - SHIFT);
                         ok = ok && (!stored || fits);
                     }
                 }
@@ -723,13 +755,17 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
 #pragma unroll
                     for (int rr = 0; rr < ROWS; ++rr)
 #pragma unroll
-                        for (int k = 0; k < CPT; ++k)  // V in the low word (|V| < 2^31), high word zero
-                            o[rr][k] = static_cast<uint32_t>(static_cast<int32_t>(fx::to_fixed(o[rr][k], -SHIFT)));
+                        for (int k = 0; k < CPT; ++k) {
+                            if constexpr (STEPS == 0)
+                                o[rr][k] = static_cast<uint64_t>(static_cast<int64_t>(V[rr][k]));
+                            else  // V in the low word, high word zero
+                                o[rr][k] = static_cast<uint32_t>(V[rr][k]);
+                        }
                 }
             }
         }
 #pragma unroll 1
-        for (int t = 0; t < STEPS; ++t) {
+        for (int t = 0; t < nsteps; ++t) {
             if (t > 0) {  // advance the whole tile, halo included: in_{k+1} = in_k + 1
                 __syncthreads();
                 if constexpr (DT == FP64) {
@@ -757,8 +793,12 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
 #pragma unroll
             for (int rr = 0; rr < ROWS; ++rr)
 #pragma unroll
-                for (int k = 0; k < CPT; ++k)
-                    o[rr][k] = from_fixed32(static_cast<int32_t>(static_cast<uint32_t>(o[rr][k])), -pow2_shift(P, R));
+                for (int k = 0; k < CPT; ++k) {
+                    if constexpr (STEPS == 0)
+                        o[rr][k] = fx::from_fixed(static_cast<int64_t>(o[rr][k]), -pow2_shift(P, R));
+                    else
+                        o[rr][k] = from_fixed32(static_cast<int32_t>(static_cast<uint32_t>(o[rr][k])), -pow2_shift(P, R));
+                }
         }
 #pragma unroll
         for (int rr = 0; rr < ROWS; ++rr) {
@@ -789,14 +829,15 @@ constexpr int min_blocks()
 template <int P, int R, int DT, int STEPS, int TH_>
 __global__ void __launch_bounds__(THREADS, min_blocks<P, R, DT, STEPS, TH_>())
     k_stencil_tile(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ CUtensorMap tm_out,
-                   const int64_t n, void* __restrict__ in_next_v, void* __restrict__ out_v, unsigned* __restrict__ status)
+                   const int64_t n, void* __restrict__ in_next_v, void* __restrict__ out_v, unsigned* __restrict__ status,
+                   const int depth, const int64_t row0)
 {
     using G = Geo<DT, R, TH_>;
     using C = Cfg<DT, TH_>;
     extern __shared__ __align__(128) unsigned char smem[];
     int* s_red = reinterpret_cast<int*>(smem + G::RED_OFF);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + G::BAR_OFF);
-    const int64_t i0 = static_cast<int64_t>(blockIdx.y) * C::TH;
+    const int64_t i0 = row0 + static_cast<int64_t>(blockIdx.y) * C::TH;
     const int64_t j0 = static_cast<int64_t>(blockIdx.x) * C::TW;
     const bool has_out = tile_has_out(i0, j0, n, R, C::TW, C::TH);
 
@@ -813,7 +854,7 @@ __global__ void __launch_bounds__(THREADS, min_blocks<P, R, DT, STEPS, TH_>())
         mbar_wait_bounded(bar, 0);  // let the copies land before the CTA's shared memory is released
         return;
     }
-    process_tile<P, R, DT, STEPS, false, TH_>(smem, s_red, i0, j0, n, has_out, in_next_v, out_v);
+    process_tile<P, R, DT, STEPS, false, TH_>(smem, s_red, i0, j0, n, has_out, in_next_v, out_v, true, depth);
 }
 
 template <int P, int R, int DT, int STEPS, int TH_>
@@ -823,14 +864,19 @@ cudaError_t launch(const Launch& L)
     using C = Cfg<DT, TH_>;
     if (cudaError_t e = cudaFuncSetAttribute(k_stencil_tile<P, R, DT, STEPS, TH_>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM))
         return e;
-    const int64_t tx = (L.n + C::TW - 1) / C::TW, ty = (L.n + C::TH - 1) / C::TH;
+    if (L.row0 < 0 || L.row0 % C::TH != 0 || L.row0 >= L.n || L.rows < 0 || (STEPS == 0 && L.depth < 1))
+        return cudaErrorInvalidValue;
+    const int64_t rows = L.rows > 0 && L.rows < L.n - L.row0 ? L.rows : L.n - L.row0;
+    const int64_t tx = (L.n + C::TW - 1) / C::TW, ty = (rows + C::TH - 1) / C::TH;
     if (ty > 65535) return cudaErrorInvalidValue;
     const dim3 grid(static_cast<unsigned>(tx), static_cast<unsigned>(ty));
-    k_stencil_tile<P, R, DT, STEPS, TH_><<<grid, THREADS, G::SMEM, L.stream>>>(L.tm_in, L.tm_out, L.n, L.in_next, L.out, L.status);
+    k_stencil_tile<P, R, DT, STEPS, TH_><<<grid, THREADS, G::SMEM, L.stream>>>(L.tm_in, L.tm_out, L.n, L.in_next, L.out,
+                                                                             L.status, L.depth, L.row0);
     return cudaGetLastError();
 }
 
-// Supported temporal depths; a run of any length is split into launches of these.
+// Supported temporal depths; a run of any length is split into launches of these, or runs in one
+// launch of the run-time-depth kernel (steps = 0, TH = 32 only).
 constexpr int MAX_STEPS = 8;
 
 template <int P, int DT, int TH_>
@@ -843,6 +889,11 @@ cudaError_t launch_pattern(int R, int steps, const Launch& L)
         case 2: return launch<P, RR, DT, 2, TH_>(L);             \
         case 4: return launch<P, RR, DT, 4, TH_>(L);             \
         case 8: return launch<P, RR, DT, 8, TH_>(L);             \
+        case 0:                                                  \
+            if constexpr (TH_ == TH_DEFAULT)                     \
+                return launch<P, RR, DT, 0, TH_>(L);             \
+            else                                                 \
+                return cudaErrorInvalidValue;                    \
         default: return cudaErrorInvalidValue;                   \
         }
     switch (R) {

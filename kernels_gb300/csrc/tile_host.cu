@@ -83,9 +83,28 @@ bool tma_depth_ok(int steps) { return steps == 1 || steps == 2 || steps == 4 || 
 
 bool tma_rows_ok(int tile_rows) { return tile_rows == tile::TH_DEFAULT || tile_rows == tile::TH_TALL; }
 
+namespace {
+cudaError_t launch_tma(const StencilCall& c, int steps, unsigned* status, int tile_rows, int depth, int64_t row0,
+                       int64_t rows);
+}  // namespace
+
 cudaError_t launch_stencil_tma(const StencilCall& c, int steps, unsigned* status, int tile_rows)
 {
     if (!tma_depth_ok(steps) || !tma_rows_ok(tile_rows)) return cudaErrorInvalidValue;
+    return launch_tma(c, steps, status, tile_rows, 0, 0, 0);
+}
+
+cudaError_t launch_stencil_tma_band(const StencilCall& c, int depth, int64_t row0, int64_t rows, unsigned* status)
+{
+    if (depth < 1 || row0 < 0 || row0 % tile::TH_DEFAULT != 0 || rows < 1) return cudaErrorInvalidValue;
+    return launch_tma(c, 0, status, tile::TH_DEFAULT, depth, row0, rows);
+}
+
+namespace {
+
+cudaError_t launch_tma(const StencilCall& c, int steps, unsigned* status, int tile_rows, int depth, int64_t row0,
+                       int64_t rows)
+{
     tile::Launch L{};
     int ix, iy, ox, oy;
     tile::boxes(c.dtype, c.R, tile_rows, &ix, &iy, &ox, &oy);
@@ -96,6 +115,9 @@ cudaError_t launch_stencil_tma(const StencilCall& c, int steps, unsigned* status
     L.out = c.out;
     L.status = status;
     L.stream = c.stream;
+    L.depth = depth;
+    L.row0 = row0;
+    L.rows = rows;
     const bool tall = tile_rows == tile::TH_TALL;
     if (c.dtype == FP64) {
         if (c.pattern == STAR) return tall ? tile::launch_fp64_star_tall(c.R, steps, L) : tile::launch_fp64_star(c.R, steps, L);
@@ -104,5 +126,7 @@ cudaError_t launch_stencil_tma(const StencilCall& c, int steps, unsigned* status
     if (c.pattern == STAR) return tall ? tile::launch_fp32c_star_tall(c.R, steps, L) : tile::launch_fp32c_star(c.R, steps, L);
     return tall ? tile::launch_fp32c_grid_tall(c.R, steps, L) : tile::launch_fp32c_grid(c.R, steps, L);
 }
+
+}  // namespace
 
 }  // namespace prk
