@@ -8,8 +8,9 @@
 // variant with a ring of stages per CTA measured slower here: fewer warps per SM to evaluate each
 // tile, and CTAs drifting apart in the raster order.)
 //
-// In a tile, lane l owns CPT adjacent columns (one 16-byte vector) and warp w owns rows w, w+8,
-// w+16, w+24. in_next and out go straight to HBM with 16-byte stores.
+// In a tile, lane l owns CPT adjacent columns (one 16-byte vector) and warp w owns the ROWS
+// consecutive rows from w * ROWS, so that the rows of a thread share their vertical taps in
+// registers. in_next and out go straight to HBM with 16-byte stores.
 //
 // Temporal depth STEPS: the tile applies STEPS consecutive applications before writing back.
 // `in` evolves pointwise (in_{k+1} = in_k + 1, Cxx11/stencil-openmp.cc:208-218), so the copy in
@@ -368,6 +369,72 @@ __device__ __forceinline__ void fexact_points(const float* v, int ld, float (&S)
     }
 }
 
+// fexact_points for the ROWS consecutive rows of a thread at once: S[rr] for the CPT points of row
+// r0 + rr, v pointing at V(r0, c0). Every row segment (star: every column strip) is read from
+// shared memory once and serves every row it is a tap of. The arithmetic is exact, so the order of
+// the terms does not matter.
+template <int P, int R, int CPT, int ROWS, int RA>
+__device__ __forceinline__ void fexact_rows(const float* v, int ld, float (&S)[ROWS][CPT])
+{
+    constexpr int SEG = CPT + 2 * RA;
+    constexpr int NR = ROWS + 2 * R;  // rows r0 - R .. r0 + ROWS - 1 + R
+    if constexpr (P == STAR) {
+        float col[NR][CPT];
+#pragma unroll
+        for (int q = 0; q < NR; ++q)
+            if (q < R || q >= R + ROWS) ld_seg2<CPT>(v + (q - R) * ld, col[q]);
+#pragma unroll
+        for (int rr = 0; rr < ROWS; ++rr) {
+            float m[SEG];
+            ld_seg2<SEG>(v + rr * ld - RA, m);
+#pragma unroll
+            for (int k = 0; k < CPT; ++k) {
+                col[rr + R][k] = m[k + RA];
+                S[rr][k] = 0.0f;
+            }
+#pragma unroll
+            for (int dc = 1; dc <= R; ++dc) {
+                const float cc = static_cast<float>(coef<P, R>(dc, 0));
+#pragma unroll
+                for (int k = 0; k < CPT; ++k)
+                    S[rr][k] = __fmaf_rn(cc, __fsub_rn(m[k + RA + dc], m[k + RA - dc]), S[rr][k]);
+            }
+        }
+#pragma unroll
+        for (int rr = 0; rr < ROWS; ++rr)
+#pragma unroll
+            for (int dr = 1; dr <= R; ++dr) {
+                const float cc = static_cast<float>(coef<P, R>(0, dr));
+#pragma unroll
+                for (int k = 0; k < CPT; ++k)
+                    S[rr][k] = __fmaf_rn(cc, __fsub_rn(col[rr + R + dr][k], col[rr + R - dr][k]), S[rr][k]);
+            }
+    } else {
+        float seg[NR][SEG];
+#pragma unroll
+        for (int q = 0; q < NR; ++q) ld_seg2<SEG>(v + (q - R) * ld - RA, seg[q]);
+#pragma unroll
+        for (int rr = 0; rr < ROWS; ++rr) {
+#pragma unroll
+            for (int k = 0; k < CPT; ++k) S[rr][k] = 0.0f;
+#pragma unroll
+            for (int dr = 0; dr <= R; ++dr)
+#pragma unroll
+                for (int dc = -R; dc <= R; ++dc) {
+                    if (dr == 0 && dc <= 0) continue;
+                    const int c = coef<P, R>(dc, dr);
+                    if (c != 0) {
+#pragma unroll
+                        for (int k = 0; k < CPT; ++k)
+                            S[rr][k] = __fmaf_rn(static_cast<float>(c),
+                                                 __fsub_rn(seg[rr + R + dr][k + RA + dc], seg[rr + R - dr][k + RA - dc]),
+                                                 S[rr][k]);
+                    }
+                }
+        }
+    }
+}
+
 // binary64 encoding of f * 2^adj for an integer-valued f (|f| < 2^24): exponent rebias and a
 // mantissa shift, no conversion instruction (those run on the binary64 pipe).
 __device__ __forceinline__ uint64_t f2d(float f, int adj)
@@ -583,7 +650,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
         __syncthreads();  // every converted word visible
     }
 
-    // Set by the multi-application FP32 route when the warp's out words are held as integers
+    // Set by the multi-application FP32 route when the tile's out words are held as integers
     bool oint = false;
 
     // S of CPT points of row r (tile coordinates) added into the out words o[] (in place)
@@ -705,7 +772,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
         // one pass: each row's new out and in_next leave as soon as they are computed
 #pragma unroll
         for (int rr = 0; rr < ROWS; ++rr) {
-            const int r = warp + WARPS * rr;
+            const int r = warp * ROWS + rr;
             const int64_t gi = i0 + r;
             if (!col_ok || gi >= n) continue;
             const bool row_out = has_out && gi >= R && gi < n - R;
@@ -724,14 +791,14 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
         bool ract[ROWS];  // the row holds interior points
 #pragma unroll
         for (int rr = 0; rr < ROWS; ++rr) {
-            const int r = warp + WARPS * rr;
+            const int r = warp * ROWS + rr;
             const int64_t gi = i0 + r;
             ract[rr] = col_ok && gi < n && has_out && gi >= R && gi < n - R;
 #pragma unroll
             for (int k = 0; k < CPT; ++k) o[rr][k] = ract[rr] ? load_out(r, k) : 0ull;
         }
         if constexpr (EXACT) {
-            // FP32 route: when every out word the warp stores is an integer V of 2^-SHIFT units with
+            // FP32 route: when every out word the tile stores is an integer V of 2^-SHIFT units with
             // |V| < 2^21, out is held as V. Every S is an integer below 2^24 units, so each binary64
             // add of the reference chain (out + S) is exact (the running V stays below 2^28 for 8
             // applications, int32, and below 2^41 for FP32_MAX_STEPS, int64) and its conversion at
@@ -750,7 +817,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
                         ok = ok && (!stored || fits);
                     }
                 }
-                oint = __all_sync(0xffffffffu, ok);
+                oint = __syncthreads_and(ok) != 0;
                 if (oint) {
 #pragma unroll
                     for (int rr = 0; rr < ROWS; ++rr)
@@ -764,6 +831,35 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
                 }
             }
         }
+        bool fast = false;  // the FP32 route with integer-held out (block-uniform)
+        if constexpr (EXACT) fast = fexact && oint;
+        if (fast) {
+            // The same applications in their tightest form: the route is fixed for the launch, and
+            // a thread's S for all its rows comes from one pass over its column strip.
+            if constexpr (EXACT) {
+                const float* sf = reinterpret_cast<const float*>(s_in) + (warp * ROWS + R) * G::SW + G::RA + c0;
+#pragma unroll 1
+                for (int t = 0; t < nsteps; ++t) {
+                    if (t > 0) {
+                        __syncthreads();
+                        advance_f32<G::ELEMS>(reinterpret_cast<float*>(s_in));
+                        __syncthreads();
+                    }
+                    float S[ROWS][CPT];
+                    fexact_rows<P, R, CPT, ROWS, G::RA>(sf, G::SW, S);
+#pragma unroll
+                    for (int rr = 0; rr < ROWS; ++rr)
+#pragma unroll
+                        for (int k = 0; k < CPT; ++k) {
+                            if constexpr (STEPS == 0)
+                                o[rr][k] += static_cast<uint64_t>(static_cast<int64_t>(__float2int_rn(S[rr][k])));
+                            else
+                                o[rr][k] = static_cast<uint32_t>(static_cast<uint32_t>(o[rr][k]) +
+                                                                 static_cast<uint32_t>(__float2int_rn(S[rr][k])));
+                        }
+                }
+            }
+        } else {
 #pragma unroll 1
         for (int t = 0; t < nsteps; ++t) {
             if (t > 0) {  // advance the whole tile, halo included: in_{k+1} = in_k + 1
@@ -787,7 +883,8 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
             }
 #pragma unroll
             for (int rr = 0; rr < ROWS; ++rr)
-                if (ract[rr]) apply_row(warp + WARPS * rr, o[rr]);
+                if (ract[rr]) apply_row(warp * ROWS + rr, o[rr]);
+        }
         }
         if (oint) {
 #pragma unroll
@@ -802,7 +899,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
         }
 #pragma unroll
         for (int rr = 0; rr < ROWS; ++rr) {
-            const int r = warp + WARPS * rr;
+            const int r = warp * ROWS + rr;
             const int64_t gi = i0 + r;
             if (!col_ok || gi >= n) continue;
             store_row(r, o[rr], has_out && gi >= R && gi < n - R);
