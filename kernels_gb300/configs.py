@@ -2,7 +2,8 @@
 case. The cases are seeded synthetic PRK fields (in = i+j, out = 0), the same shapes as:
 
   sweep   star and grid, R = 1..5, n = 32768, 50 iterations, FP64 and FP32C (tuned depth each, or
-          the TMA kernel at --depth D without tuning):
+          the TMA kernel at --depth D without tuning; --depth 0: every timed application in one
+          launch):
           PRK GFLOP/s, algorithmic HBM GB/s and its fraction of the measured peak, the norm check,
           and the FP32C relative error against the FP64 result (bit-identical to the reference's)
   large   star R=4, FP32C at n = 65536 and FP64 at n = 46000, 200 iterations, tuned depth
@@ -50,12 +51,13 @@ def one_case(torch, pattern: int, r: int, n: int, iterations: int, dtype: int, p
     if depth is None:
         tuning = kg.tune(pattern, r, n, dtype)
     else:
-        tuning = {"depth": depth, "kernel": "fixed", "tile_rows": 32, "tile_cols": 0, "cols_per_thread": 0}
+        tuning = {"depth": depth or iterations, "kernel": "whole" if depth == 0 else "fixed", "tile_rows": 32,
+                  "tile_cols": 0, "cols_per_thread": 0}
     t0 = time.perf_counter()
     if depth is None:
         res = kg.run(pattern, r, iterations, in_a, in_b, out, tuned=True)
     else:
-        res = kg.run(pattern, r, iterations, in_a, in_b, out, depth=depth)
+        res = kg.run(pattern, r, iterations, in_a, in_b, out, depth=depth or 1, whole=depth == 0)
     wall = time.perf_counter() - t0
     nrm = kg.norm(r, out)
     idx = torch.tensor([i * n + j for i, j in pts], device="cuda")

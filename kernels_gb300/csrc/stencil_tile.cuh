@@ -501,6 +501,25 @@ __device__ __forceinline__ void advance_f32(float* p)
     }
 }
 
+// dst = src + 1 over the whole staged FP32 tile (the double-buffered FP32 route)
+template <int ELEMS>
+__device__ __forceinline__ void advance_f32_to(const float* src, float* dst)
+{
+    constexpr int NV = ELEMS / 4;
+#pragma unroll
+    for (int q = 0; q < (NV + THREADS - 1) / THREADS; ++q) {
+        const int idx = threadIdx.x + q * THREADS;
+        if (NV % THREADS == 0 || idx < NV) {
+            float4 v = reinterpret_cast<const float4*>(src)[idx];
+            v.x = __fadd_rn(v.x, 1.0f);
+            v.y = __fadd_rn(v.y, 1.0f);
+            v.z = __fadd_rn(v.z, 1.0f);
+            v.w = __fadd_rn(v.w, 1.0f);
+            reinterpret_cast<float4*>(dst)[idx] = v;
+        }
+    }
+}
+
 template <int ELEMS>
 __device__ __forceinline__ void advance_i64(int64_t* p, int64_t one)
 {
@@ -652,6 +671,8 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
 
     // Set by the multi-application FP32 route when the tile's out words are held as integers
     bool oint = false;
+    // Offset in floats of the FP32 tile holding the last application's in (double-buffered route)
+    int fin_off = 0;
 
     // S of CPT points of row r (tile coordinates) added into the out words o[] (in place)
     auto apply_row = [&](int r, uint64_t* o) {
@@ -721,7 +742,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
         bool done = false;
         if constexpr (EXACT) {
             if (fexact) {
-                const float* v = reinterpret_cast<const float*>(s_in) + soff;
+                const float* v = reinterpret_cast<const float*>(s_in) + fin_off + soff;
 #pragma unroll
                 for (int k = 0; k < CPT; ++k) nxt[k] = as_dbl(f2d(__fadd_rn(v[k], 1.0f), 0));
                 done = true;
@@ -835,18 +856,22 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
         if constexpr (EXACT) fast = fexact && oint;
         if (fast) {
             // The same applications in their tightest form: the route is fixed for the launch, and
-            // a thread's S for all its rows comes from one pass over its column strip.
+            // a thread's S for all its rows comes from one pass over its column strip. The FP32
+            // tile takes half of the binary64 stage, so the other half holds the next
+            // application's in: while application t reads one, in + 1 is written to the other, and
+            // one barrier per application separates them.
             if constexpr (EXACT) {
-                const float* sf = reinterpret_cast<const float*>(s_in) + (warp * ROWS + R) * G::SW + G::RA + c0;
+                float* const buf = reinterpret_cast<float*>(s_in);
+                const int own = (warp * ROWS + R) * G::SW + G::RA + c0;
 #pragma unroll 1
                 for (int t = 0; t < nsteps; ++t) {
-                    if (t > 0) {
-                        __syncthreads();
-                        advance_f32<G::ELEMS>(reinterpret_cast<float*>(s_in));
+                    const int cur = (t & 1) * G::ELEMS;
+                    float S[ROWS][CPT];
+                    fexact_rows<P, R, CPT, ROWS, G::RA>(buf + cur + own, G::SW, S);
+                    if (t + 1 < nsteps) {
+                        advance_f32_to<G::ELEMS>(buf + cur, buf + (G::ELEMS - cur));
                         __syncthreads();
                     }
-                    float S[ROWS][CPT];
-                    fexact_rows<P, R, CPT, ROWS, G::RA>(sf, G::SW, S);
 #pragma unroll
                     for (int rr = 0; rr < ROWS; ++rr)
 #pragma unroll
@@ -858,6 +883,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
                                                                  static_cast<uint32_t>(__float2int_rn(S[rr][k])));
                         }
                 }
+                fin_off = ((nsteps - 1) & 1) * G::ELEMS;
             }
         } else {
 #pragma unroll 1
@@ -917,7 +943,9 @@ constexpr int min_blocks()
     if (DT == FP64 && !pow2_weights(P, R)) return STEPS == 1 ? 2 : 1;
     if (DT == FP32C && P == GRID && R >= 3) return 2;  // bound by FP32 issue: registers over residency
     const int b = Geo<DT, R, TH_>::CTAS;
-    return STEPS == 1 ? b : (b < 3 ? b : 3);
+    if (STEPS == 1) return b;
+    const int cap = DT == FP64 ? 4 : 3;  // FP64 power-of-two: the FP32 route is shared-memory bound
+    return b < cap ? b : cap;
 }
 
 // One CTA per tile: blockIdx = (tile column, tile row). The elected thread issues the tile's two TMA
