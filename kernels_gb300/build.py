@@ -88,6 +88,8 @@ def build_oracle() -> None:
     ref = Path(os.environ.get("PRK_REFERENCE", "/root/reference"))
     if (ref / "Cxx11" / "stencil_seq.hpp").exists():
         _run(["make", "-s", "-C", str(ROOT / "oracle"), "ref", f"REF={ref}"])
+    if (ref / "Cxx11" / "stencil-cuda.cu").exists():
+        _run(["make", "-s", "-C", str(ROOT / "oracle"), "ref-cuda", f"REF={ref}"])
 
 
 if __name__ == "__main__":
