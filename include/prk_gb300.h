@@ -156,7 +156,8 @@ int prk_gb300_status(void);
  * $HOME/.cache/prk_gb300/tune.jsonl. No counterpart in the reference (whose tile size is a CLI
  * argument, Cxx11/stencil-openmp.cc:111-116). */
 typedef struct {
-    int depth;                      /* applications per launch: 1, 2, 4 or 8 */
+    int depth;                      /* applications per launch: 1, 2, 4 or 8; 0: every timed
+                                       application in one launch (PRK_RUN_WHOLE) */
     int kernel;                     /* 1 = generic kernels, 2 = TMA tile kernels, 3 = batched kernel */
     int tile_rows;                  /* tile shape (rows x columns) of the chosen kernel */
     int tile_cols;

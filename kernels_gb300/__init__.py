@@ -192,7 +192,8 @@ def run_host(pattern: int, radius: int, iterations: int, h_in, h_out, h_in_final
 
 def tune(pattern: int, radius: int, n: int, dtype: int = FP64, batch: bool = False, force: bool = False) -> dict:
     """The autotuner's choice for (pattern, radius, n, dtype): kernel family, tile shape, thread
-    coarsening and temporal depth, measured on scratch buffers and cached (prk_gb300_tune)."""
+    coarsening and temporal depth (0: the whole run in one launch), measured on scratch buffers and
+    cached (prk_gb300_tune)."""
     from ._lib import Tuning
     t = Tuning()
     check(load().prk_gb300_tune(pattern, radius, n, dtype, (1 if batch else 0) | (2 if force else 0), C.byref(t)))

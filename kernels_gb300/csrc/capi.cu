@@ -268,7 +268,7 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
     if (iterations < 1) return fail(PRK_ERR_ARG, "iterations must be >= 1");
     const bool unfused = (flags & PRK_RUN_UNFUSED) != 0;
     const bool graph = (flags & PRK_RUN_GRAPH) != 0;
-    const bool whole = (flags & PRK_RUN_WHOLE) != 0;
+    bool whole = (flags & PRK_RUN_WHOLE) != 0;
     if (whole && unfused) return fail(PRK_ERR_ARG, "PRK_RUN_WHOLE is a fused form");
     int depth = (flags >> 8) & 0xFF;
     if (depth == 0) depth = 1;
@@ -279,7 +279,8 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
     if ((flags & PRK_RUN_TUNED) && !unfused && !whole) {
         prk_gb300_tuning t{};
         if (int rc = prk_gb300_tune(pattern, radius, n, dtype, 0, &t)) return rc;
-        depth = t.depth;
+        depth = t.depth > 0 ? t.depth : 1;
+        whole = t.depth == 0;
         tuned_generic = t.kernel == 1;
         if (!tuned_generic) rows = t.tile_rows;
     }

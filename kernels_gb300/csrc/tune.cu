@@ -2,8 +2,8 @@
 // n, dtype) on scratch buffers and keeps the fastest in memory and in a JSON-lines cache file.
 //
 // Candidates, single grid: the TMA tile kernels with tiles of 32 and of 64 rows (4 or 8 rows per
-// thread) at temporal depth 1, 2, 4 and 8 (when the shape allows TMA: n a multiple of the vector
-// width), and the generic kernels. Batched grids: the batched kernel at depth 1, 2, 4 and 8. Every candidate computes the same bits (FP64) or stays within the
+// thread) at temporal depth 1, 2, 4 and 8 and with the whole run in one launch (when the shape
+// allows TMA: n a multiple of the vector width), and the generic kernels. Batched grids: the batched kernel at depth 1, 2, 4 and 8. Every candidate computes the same bits (FP64) or stays within the
 // FP32C bound, so the choice affects speed only.
 #include <cstdio>
 #include <cstdlib>
@@ -136,7 +136,7 @@ extern "C" int prk_gb300_tune(int pattern, int radius, int64_t n, int dtype, int
     if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess)
         return err(PRK_ERR_STATE, "tune: no CUDA device");
     char keybuf[512];
-    std::snprintf(keybuf, sizeof keybuf, "%s|sm%d%d|%s|R%d|%s|n%lld|%s%s", prop.name, prop.major, prop.minor,
+    std::snprintf(keybuf, sizeof keybuf, "%s|sm%d%d|%s|R%d|%s|n%lld|%s%s|v2", prop.name, prop.major, prop.minor,
                   pattern == PRK_STAR ? "star" : "grid", radius, dtype == PRK_FP64 ? "fp64" : "fp32c",
                   static_cast<long long>(bucket(n)), batch ? "batch" : "single", tma_shape ? "" : "|generic");
     const std::string key = keybuf;
@@ -184,6 +184,11 @@ extern "C" int prk_gb300_tune(int pattern, int radius, int64_t n, int dtype, int
                 if (batch) best.kernel = 3;
             }
         }
+    }
+    if (!rc && !batch && tma_shape) {  // the whole run in one launch
+        double sec = 0.0;
+        rc = time_run(pattern, radius, m, dtype, PRK_RUN_WHOLE, s, &sec);
+        if (!rc && sec < best.seconds_per_application) best = prk_gb300_tuning{0, 2, th, tw, cpt, sec, 0};
     }
     if (!rc && !batch && tma_shape) {  // the generic kernels, depth 1
         double sec = 0.0;

@@ -94,7 +94,7 @@ def test_batch_rejects_bad_grids(cuda):
 
 def test_tuner_choice_is_cached_and_used(cuda, tmp_path, monkeypatch):
     t1 = kg.tune(kg.STAR, 2, 1024, kg.FP64, force=True)
-    assert t1["depth"] in (1, 2, 4, 8) and t1["kernel"] in ("tma", "generic")
+    assert t1["depth"] in (0, 1, 2, 4, 8) and t1["kernel"] in ("tma", "generic")  # 0: whole run in one launch
     assert t1["seconds_per_application"] > 0 and not t1["from_cache"]
     t2 = kg.tune(kg.STAR, 2, 1024, kg.FP64)
     assert t2["from_cache"] and t2["depth"] == t1["depth"]
