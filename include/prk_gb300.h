@@ -191,8 +191,9 @@ typedef struct {
 typedef struct prk_gb300_batch prk_gb300_batch;
 
 /* Builds a batch over `count` grids of one dtype (the descriptors are copied; the buffers stay
- * caller-owned). flags: PRK_RUN_DEPTH(d) fixes the temporal depth of every grid; PRK_BATCH_TUNED
- * takes each grid's depth from the autotuner (prk_gb300_tune), grouping grids by depth. Allocates
+ * caller-owned). flags: PRK_RUN_DEPTH(d) fixes the temporal depth of every grid; PRK_RUN_WHOLE
+ * runs every grid's timed applications in one launch; PRK_BATCH_TUNED takes each grid's depth
+ * (0 for the whole run) from the autotuner (prk_gb300_tune), grouping grids by depth. Allocates
  * the batch's device tables. */
 #define PRK_BATCH_TUNED 0x10000
 int prk_gb300_batch_create(const prk_gb300_grid* grids, int count, int dtype, int flags, prk_gb300_batch** batch);

@@ -205,9 +205,10 @@ def tune(pattern: int, radius: int, n: int, dtype: int = FP64, batch: bool = Fal
 class Batch:
     """Many independent grids advanced together by the batched persistent kernel
     (prk_gb300_batch_*). `grids` is a list of (pattern, radius, in_a, in_b, out) with device tensors;
-    all of one dtype. depth fixes the temporal depth; tuned=True takes it per grid from the tuner."""
+    all of one dtype. depth fixes the temporal depth; whole=True runs every grid's timed applications
+    in one launch; tuned=True takes the depth per grid from the tuner."""
 
-    def __init__(self, grids, depth: int | None = None, tuned: bool = False):
+    def __init__(self, grids, depth: int | None = None, tuned: bool = False, whole: bool = False):
         from ._lib import Grid
         if not grids:
             raise PrkError(-1, "a batch needs at least one grid")
@@ -220,7 +221,7 @@ class Batch:
                 raise PrkError(-1, "all grids of a batch share one dtype")
             _check_out(out, n, dt)
             arr[k] = Grid(pattern, radius, n, in_a.data_ptr(), in_b.data_ptr(), out.data_ptr())
-        flags = (depth or 0) << 8 | (0x10000 if tuned else 0)
+        flags = (depth or 0) << 8 | (0x10000 if tuned else 0) | (RUN_WHOLE if whole else 0)
         h = C.c_void_p()
         check(load().prk_gb300_batch_create(arr, len(grids), dt, flags, C.byref(h)))
         self._h = h

@@ -1,4 +1,4 @@
-// Instantiations of the batched kernel for fp32c storage, temporal depths 1, 2, 4, 8.
+// Instantiations of the batched kernel for fp32c storage, temporal depths 1, 2, 4, 8 and run-time depth.
 #include "batch_kernel.cuh"
 
 namespace prk {
@@ -15,6 +15,7 @@ int ctas_per_sm_fp32c(int steps)
     case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<FP32C, 2>, tile::THREADS, Layout<FP32C>::SMEM); break;
     case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<FP32C, 4>, tile::THREADS, Layout<FP32C>::SMEM); break;
     case 8: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<FP32C, 8>, tile::THREADS, Layout<FP32C>::SMEM); break;
+    case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<FP32C, 0>, tile::THREADS, Layout<FP32C>::SMEM); break;
     }
     return e == cudaSuccess ? b : 0;
 }

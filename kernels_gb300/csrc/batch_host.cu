@@ -25,7 +25,7 @@ int cuda_err(cudaError_t e, const char* what)
 
 // Grids advanced by one kernel sequence: all of one temporal depth.
 struct Group {
-    int depth = 1;
+    int depth = 1;                     // applications per launch; 0: the rest of the run in one launch
     std::vector<int> members;          // indices into the batch's grid list
     GridDesc* d_desc = nullptr;        // device descriptors
     int64_t* d_off = nullptr;          // device tile offsets (members + 1)
@@ -93,17 +93,29 @@ int build_tables(prk_gb300_batch* b, const std::vector<int>& members, GridDesc**
     return PRK_OK;
 }
 
+// steps 1, 2, 4 or 8: a launch of that depth; steps 0: one launch of `apps` applications.
 cudaError_t launch_group(const prk_gb300_batch* b, const GridDesc* desc, const int64_t* off, int ngrids, int64_t total,
-                         int depth, int slot, int parity, cudaStream_t s)
+                         int steps, int slot, int parity, cudaStream_t s, int apps = 0)
 {
-    prk::batch::Launch L{desc, off, ngrids, total, b->d_queue + slot, parity, b->ctas, s};
-    return b->dtype == PRK_FP64 ? prk::batch::launch_fp64(depth, L) : prk::batch::launch_fp32c(depth, L);
+    prk::batch::Launch L{desc, off, ngrids, total, b->d_queue + slot, parity, b->ctas, s, apps};
+    return b->dtype == PRK_FP64 ? prk::batch::launch_fp64(steps, L) : prk::batch::launch_fp32c(steps, L);
+}
+
+// Applications of a group's next launch with `left` to go: the whole rest for depth 0, else the
+// group depth, the remainder in powers of two.
+int next_apps(int depth, int left)
+{
+    if (depth == 0) return left;
+    int d = depth;
+    while (d > left) d >>= 1;
+    return d;
 }
 
 int launches_of(const prk_gb300_batch* b, int iterations)
 {
     int total = 0;
-    for (const Group& g : b->groups) total += (iterations + g.depth - 1) / g.depth + 2;  // remainder split in powers of 2
+    for (const Group& g : b->groups)
+        total += g.depth == 0 ? 1 : (iterations + g.depth - 1) / g.depth + 2;  // remainder split in powers of 2
     return total;
 }
 
@@ -117,10 +129,10 @@ int enqueue_timed(prk_gb300_batch* b, int iterations, cudaStream_t s, std::vecto
         Group& g = b->groups[gi];
         int parity = 1, left = iterations;
         while (left > 0) {
-            int d = g.depth;
-            while (d > left) d >>= 1;
+            const int d = next_apps(g.depth, left);
             if (slot >= b->queue_slots) return err(PRK_ERR_STATE, "batch: more launches than queue slots");
-            cudaError_t e = launch_group(b, g.d_desc, g.d_off, static_cast<int>(g.members.size()), g.total, d, slot++, parity, s);
+            cudaError_t e = launch_group(b, g.d_desc, g.d_off, static_cast<int>(g.members.size()), g.total,
+                                         g.depth == 0 ? 0 : d, slot++, parity, s, d);
             if (e != cudaSuccess) return cuda_err(e, "batch launch");
             parity ^= 1;
             left -= d;
@@ -143,6 +155,7 @@ int prk_gb300_batch_create(const prk_gb300_grid* grids, int count, int dtype, in
     int depth = (flags >> 8) & 0xFF;
     if (depth == 0) depth = 1;
     if (!prk::tma_depth_ok(depth)) return err(PRK_ERR_ARG, "batch: temporal depth is not 1, 2, 4 or 8");
+    if (flags & PRK_RUN_WHOLE) depth = 0;
     for (int k = 0; k < count; ++k) {
         const prk_gb300_grid& g = grids[k];
         if ((g.pattern != PRK_STAR && g.pattern != PRK_GRID) || g.radius < 1 || g.radius > prk::RMAX || g.n < 1 ||
@@ -235,10 +248,8 @@ int prk_gb300_batch_run(prk_gb300_batch* b, int iterations, int flags, double* e
                 for (size_t gi = 0; gi < b->groups.size(); ++gi) {  // same launch sequence as captured
                     int p = 1, left = iterations;
                     while (left > 0) {
-                        int d = b->groups[gi].depth;
-                        while (d > left) d >>= 1;
                         p ^= 1;
-                        left -= d;
+                        left -= next_apps(b->groups[gi].depth, left);
                     }
                     parity[gi] = p;
                 }
@@ -291,10 +302,8 @@ int prk_gb300_batch_launches(const prk_gb300_batch* b, int iterations)
     for (const Group& g : b->groups) {
         int left = iterations;
         while (left > 0) {
-            int d = g.depth;
-            while (d > left) d >>= 1;
             ++total;
-            left -= d;
+            left -= next_apps(g.depth, left);
         }
     }
     return total;

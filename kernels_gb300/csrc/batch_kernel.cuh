@@ -9,8 +9,9 @@
 // evaluated by the same code as the TMA kernels (stencil_tile.cuh), with the pattern and radius
 // picked per item by a switch.
 //
-// Every launch advances all grids of the launch by STEPS applications (temporal depth), ping-ponging
-// between each grid's two `in` buffers; `parity` says which one holds the current `in`.
+// Every launch advances all grids of the launch by STEPS applications (temporal depth; STEPS = 0
+// takes `depth` at run time, for a whole run in one launch), ping-ponging between each grid's two
+// `in` buffers; `parity` says which one holds the current `in`.
 #pragma once
 
 #include "stencil_tile.cuh"
@@ -48,7 +49,8 @@ struct Layout {
 
 // One work item: load the tile of grid g at `parity`, then evaluate it.
 template <int P, int R, int DT, int STEPS>
-__device__ __forceinline__ void item(unsigned char* smem, int* s_red, const GridDesc& g, int64_t t, int parity)
+__device__ __forceinline__ void item(unsigned char* smem, int* s_red, const GridDesc& g, int64_t t, int parity,
+                                     int depth)
 {
     using G = tile::Geo<DT, R>;
     using C = tile::Cfg<DT>;
@@ -74,14 +76,15 @@ __device__ __forceinline__ void item(unsigned char* smem, int* s_red, const Grid
     }
     __syncthreads();
     tile::process_tile<P, R, DT, STEPS, true>(smem, s_red, i0, j0, n, tile::tile_has_out(i0, j0, n, R, C::TW, C::TH),
-                                               g.in[parity ^ 1], g.out, g.vec_ok != 0);
+                                               g.in[parity ^ 1], g.out, g.vec_ok != 0, depth);
 }
 
 template <int DT, int STEPS>
-__device__ __forceinline__ void dispatch(unsigned char* smem, int* s_red, const GridDesc& g, int64_t t, int parity)
+__device__ __forceinline__ void dispatch(unsigned char* smem, int* s_red, const GridDesc& g, int64_t t, int parity,
+                                         int depth)
 {
 #define PRK_ITEM(PP, RR) \
-    case RR: item<PP, RR, DT, STEPS>(smem, s_red, g, t, parity); break;
+    case RR: item<PP, RR, DT, STEPS>(smem, s_red, g, t, parity, depth); break;
     if (g.pattern == STAR) {
         switch (g.R) { PRK_ITEM(STAR, 1) PRK_ITEM(STAR, 2) PRK_ITEM(STAR, 3) PRK_ITEM(STAR, 4) PRK_ITEM(STAR, 5) }
     } else {
@@ -93,7 +96,7 @@ __device__ __forceinline__ void dispatch(unsigned char* smem, int* s_red, const 
 template <int DT, int STEPS>
 __global__ void __launch_bounds__(tile::THREADS, 2)
     k_batch(const GridDesc* __restrict__ grids, const int64_t* __restrict__ tile_off, int ngrids, int64_t total,
-            unsigned long long* __restrict__ queue, int parity)
+            unsigned long long* __restrict__ queue, int parity, int depth)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ long long s_item;
@@ -110,7 +113,7 @@ __global__ void __launch_bounds__(tile::THREADS, 2)
             else hi = mid;
         }
         const GridDesc g = grids[lo];
-        dispatch<DT, STEPS>(smem, s_red, g, it - tile_off[lo], parity);
+        dispatch<DT, STEPS>(smem, s_red, g, it - tile_off[lo], parity, depth);
         __syncthreads();  // shared memory and s_item are reused by the next item
     }
 }
@@ -124,6 +127,7 @@ struct Launch {
     int parity;
     int ctas;  // persistent CTAs
     cudaStream_t stream;
+    int depth;  // applications of a run-time-depth launch (STEPS = 0)
 };
 
 template <int DT, int STEPS>
@@ -131,8 +135,9 @@ cudaError_t launch(const Launch& L)
 {
     if (cudaError_t e = cudaFuncSetAttribute(k_batch<DT, STEPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, Layout<DT>::SMEM))
         return e;
+    if (STEPS == 0 && L.depth < 1) return cudaErrorInvalidValue;
     k_batch<DT, STEPS><<<L.ctas, tile::THREADS, Layout<DT>::SMEM, L.stream>>>(L.grids, L.tile_off, L.ngrids, L.total,
-                                                                             L.queue, L.parity);
+                                                                             L.queue, L.parity, L.depth);
     return cudaGetLastError();
 }
 
@@ -144,6 +149,7 @@ cudaError_t launch_depth(int steps, const Launch& L)
     case 2: return launch<DT, 2>(L);
     case 4: return launch<DT, 4>(L);
     case 8: return launch<DT, 8>(L);
+    case 0: return launch<DT, 0>(L);
     }
     return cudaErrorInvalidValue;
 }

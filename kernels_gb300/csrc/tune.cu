@@ -3,8 +3,9 @@
 //
 // Candidates, single grid: the TMA tile kernels with tiles of 32 and of 64 rows (4 or 8 rows per
 // thread) at temporal depth 1, 2, 4 and 8 and with the whole run in one launch (when the shape
-// allows TMA: n a multiple of the vector width), and the generic kernels. Batched grids: the batched kernel at depth 1, 2, 4 and 8. Every candidate computes the same bits (FP64) or stays within the
-// FP32C bound, so the choice affects speed only.
+// allows TMA: n a multiple of the vector width), and the generic kernels. Batched grids: the
+// batched kernel at depth 1, 2, 4 and 8 and with the whole run in one launch. Every candidate
+// computes the same bits (FP64) or stays within the FP32C bound, so the choice affects speed only.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -109,7 +110,7 @@ int time_batch(int pattern, int R, int64_t m, int dtype, int depth, Scratch& s, 
     if (int rc = prk_gb300_init(m, dtype, s.p[0], s.p[2], nullptr)) return rc;
     prk_gb300_grid g{pattern, R, m, s.p[0], s.p[1], s.p[2]};
     prk_gb300_batch* b = nullptr;
-    if (int rc = prk_gb300_batch_create(&g, 1, dtype, PRK_RUN_DEPTH(depth), &b)) return rc;
+    if (int rc = prk_gb300_batch_create(&g, 1, dtype, depth > 0 ? PRK_RUN_DEPTH(depth) : PRK_RUN_WHOLE, &b)) return rc;
     double el = 0.0;
     const int apps = 16;
     int rc = prk_gb300_batch_run(b, apps, 0, &el, nullptr);
@@ -189,6 +190,11 @@ extern "C" int prk_gb300_tune(int pattern, int radius, int64_t n, int dtype, int
         double sec = 0.0;
         rc = time_run(pattern, radius, m, dtype, PRK_RUN_WHOLE, s, &sec);
         if (!rc && sec < best.seconds_per_application) best = prk_gb300_tuning{0, 2, th, tw, cpt, sec, 0};
+    }
+    if (!rc && batch) {  // the batched kernel with the whole run in one launch
+        double sec = 0.0;
+        rc = time_batch(pattern, radius, m, dtype, 0, s, &sec);
+        if (!rc && sec < best.seconds_per_application) best = prk_gb300_tuning{0, 3, th, tw, cpt, sec, 0};
     }
     if (!rc && !batch && tma_shape) {  // the generic kernels, depth 1
         double sec = 0.0;

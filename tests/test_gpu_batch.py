@@ -53,6 +53,31 @@ def test_mixed_batch_fp64_bit_exact(cuda, depth, graph):
     b.close()
 
 
+@pytest.mark.parametrize("graph", [False, True])
+def test_mixed_batch_whole_run_fp64_bit_exact(cuda, graph):
+    """Every grid's timed applications in one launch of the batched kernel."""
+    k = 9
+    b, grids = make_batch(cuda, VALID, kg.FP64, whole=True)
+    assert b.launches(k) == 1
+    b.run(k, graph=graph)
+    check_fp64(b, grids, VALID, k)
+    assert all(abs(x - 2.0 * (k + 1)) <= 1e-8 for x in b.norms())
+    b.close()
+
+
+def test_mixed_batch_whole_run_fp32c_bound(cuda):
+    k = 12
+    b, grids = make_batch(cuda, VALID, kg.FP32C, whole=True)
+    b.run(k, graph=True)
+    for (p, r, n), g in zip(VALID, grids):
+        _, ref = po.run(p, r, n, k)
+        got = g[4].cpu().numpy().astype(np.float64)
+        got = got[..., 0] + got[..., 1]
+        inner = (slice(r, n - r), slice(r, n - r))
+        assert (np.abs(got[inner] - ref[inner]) / np.abs(ref[inner])).max() <= 1e-6, (p, r, n)
+    b.close()
+
+
 def test_mixed_batch_fp32c_bound(cuda):
     k = 12
     b, grids = make_batch(cuda, VALID, kg.FP32C, depth=4)
