@@ -331,16 +331,19 @@ def run_gb300(args) -> None:
         h_in = torch.empty((n, n), dtype=torch.float64).pin_memory()
         h_out = torch.zeros((n, n), dtype=torch.float64).pin_memory()
         h_in.copy_(torch.arange(n, dtype=torch.float64)[:, None] + torch.arange(n, dtype=torch.float64)[None, :])
-        kg.run_host(pattern, r, 1, h_in, h_out)  # warm-up call (allocator, module load)
-        te, ev, norms = 0.0, 0.0, []
-        for _ in range(args.e2e_steps):  # out starts at zero for every step, outside the timed region
-            h_out.zero_()
+        # Warm-up call (allocator, module load), then the timed calls back to back: the host link
+        # drops to a slower state after about half a second without traffic, and a pause between
+        # calls (re-zeroing out on the host) would time its wake-up. out accumulates instead: every
+        # call adds 2(K+1) to each interior point, so its norm is known.
+        kg.run_host(pattern, r, 1, h_in, h_out)
+        te, ev, norm_ok = 0.0, 0.0, True
+        for step in range(args.e2e_steps):
             barrier()
             t0 = time.perf_counter()
             res = kg.run_host(pattern, r, e2e_iters, h_in, h_out)
             te += max_over_ranks(time.perf_counter() - t0)
             ev += res["kernel_s"]
-            norms.append(res["norm"])
+            norm_ok &= abs(res["norm"] - (4.0 + 2.0 * (e2e_iters + 1) * (step + 1))) <= 1e-8
         steps_e = args.e2e_steps
         e2e = {"value": round(world * fl * (e2e_iters + 1) * steps_e / te / 1e9, 3), "unit": "GFLOP/s",
                "h2d_bytes_per_step": 2 * n * n * 8, "d2h_bytes_per_step": n * n * 8 + 8,
@@ -349,7 +352,7 @@ def run_gb300(args) -> None:
                        f"and its out copied back, overlapped across bands; device norm",
                "steps": steps_e, "seconds_per_step": round(te / steps_e, 4),
                "evaluation_seconds_per_step": round(ev / steps_e, 4),
-               "norm_ok": all(abs(x - 2.0 * (e2e_iters + 1)) <= 1e-8 for x in norms)}
+               "norm_ok": bool(norm_ok)}
 
     peak, peak_kind = hbm_peak()
     b64 = algorithmic_bytes(n, r, True)
