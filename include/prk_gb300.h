@@ -221,8 +221,21 @@ int prk_gb300_batch_destroy(prk_gb300_batch* batch);
  * PRK_ERR_TIMEOUT when the timeout path works. The GPU stays usable; nothing faults or hangs. */
 int prk_gb300_selftest_timeout(void);
 
-/* Frees the device buffers prk_gb300_run_host keeps on the current device. */
+/* Frees the device buffers and streams prk_gb300_run_host keeps on the current device. */
 int prk_gb300_release(void);
+
+/* ---- Neighbouring PRK kernels on the same bandwidth roofline ---------------------------------
+ * One application per call on caller-owned device memory, stream-ordered, binary64 with every
+ * product and sum rounded on its own in the reference's order. */
+
+/* The STREAM triad A[i] += B[i] + scalar * C[i] for i < length (replaces the nstream kernel of
+ * Cxx11/nstream-cuda.cu:68-76 and its launch at :164-176). A must not overlap B or C. */
+int prk_gb300_nstream(int64_t length, double scalar, double* A, const double* B, const double* C, void* stream);
+
+/* B += A^T, then A += 1, for order x order row-major matrices (replaces transposeNoBankConflict<true>
+ * of Cxx11/transpose-cuda.cu:63-86 and its launch at :223-246; any order up to 65535 * 64, not only
+ * multiples of the tile). A and B must not overlap. */
+int prk_gb300_transpose(int64_t order, double* A, double* B, void* stream);
 
 /* Bytes one buffer of the given role needs: role 0 = in / in_next, role 1 = out. */
 int64_t prk_gb300_bytes(int64_t n, int dtype, int role);

@@ -190,6 +190,28 @@ def run_host(pattern: int, radius: int, iterations: int, h_in, h_out, h_in_final
     return {"norm": nrm.value, "elapsed_s": el.value, "kernel_s": ks.value}
 
 
+def nstream(A, B, C_, scalar: float = 3.0, stream=None) -> None:
+    """A += B + scalar * C on float64 device vectors of one length (prk_gb300_nstream)."""
+    for t in (A, B, C_):
+        if t.dtype != torch_float64() or not t.is_cuda or not t.is_contiguous() or t.numel() != A.numel():
+            raise ValueError("nstream: A, B and C must be contiguous float64 CUDA tensors of one length")
+    check(load().prk_gb300_nstream(A.numel(), scalar, A.data_ptr(), B.data_ptr(), C_.data_ptr(), _stream(stream)))
+
+
+def transpose(A, B, stream=None) -> None:
+    """B += A^T, then A += 1, on square float64 device matrices (prk_gb300_transpose)."""
+    for t in (A, B):
+        if t.dtype != torch_float64() or not t.is_cuda or not t.is_contiguous() or t.dim() != 2 \
+                or t.shape[0] != t.shape[1] or t.shape != A.shape:
+            raise ValueError("transpose: A and B must be square contiguous float64 CUDA tensors of one order")
+    check(load().prk_gb300_transpose(A.shape[0], A.data_ptr(), B.data_ptr(), _stream(stream)))
+
+
+def torch_float64():
+    import torch
+    return torch.float64
+
+
 def tune(pattern: int, radius: int, n: int, dtype: int = FP64, batch: bool = False, force: bool = False) -> dict:
     """The autotuner's choice for (pattern, radius, n, dtype): kernel family, tile shape, thread
     coarsening and temporal depth (0: the whole run in one launch), measured on scratch buffers and

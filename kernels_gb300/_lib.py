@@ -42,6 +42,8 @@ SIGNATURES: dict[str, tuple] = {
     "prk_gb300_batch_launches": (_int, [_vp, _int]),
     "prk_gb300_batch_destroy": (_int, [_vp]),
     "prk_gb300_release": (_int, []),
+    "prk_gb300_nstream": (_int, [_i64, _dbl, _vp, _vp, _vp, _vp]),
+    "prk_gb300_transpose": (_int, [_i64, _vp, _vp, _vp]),
     "prk_gb300_bytes": (_i64, [_i64, _int, _int]),
     "prk_gb300_flops": (_dbl, [_int, _int, _i64]),
     "prk_gb300_last_error": (C.c_char_p, []),

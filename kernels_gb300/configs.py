@@ -9,6 +9,10 @@ case. The cases are seeded synthetic PRK fields (in = i+j, out = 0), the same sh
   large   star R=4, FP32C at n = 65536 and FP64 at n = 46000, 200 iterations, tuned depth
   batch   the seeded 256-grid batch (kernels_gb300.workloads), FP64 and FP32C, one CUDA graph, tuned
           depth per grid (or --depth D for every grid)
+  neighbours  nstream (length 2^28, the reference's A = 0, B = C = 2, scalar 3) and transpose
+          (order 16384, A[j][i] = order*j + i, B = 0), 20 timed iterations after one untimed:
+          HBM GB/s as the reference rates them (32 B per element and iteration for both) and its
+          fraction of the measured peak; validation by the reference's own formulas, on the GPU
 
   python -m kernels_gb300.configs sweep|large|batch [--n N] [--iterations K] [--radii 1,2,...] [--depth D]
 """
@@ -122,10 +126,52 @@ def run_batch(torch, iterations: int, depth: int | None, count: int):
         torch.cuda.empty_cache()
 
 
+def run_neighbours(torch, iterations: int) -> None:
+    """nstream and transpose timed with CUDA events; validated on the device."""
+    k = iterations
+    length = 1 << 28
+    A = torch.zeros(length, dtype=torch.float64, device="cuda")
+    B = torch.full((length,), 2.0, dtype=torch.float64, device="cuda")
+    C = torch.full((length,), 2.0, dtype=torch.float64, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kg.nstream(A, B, C, scalar=3.0)  # iteration 0, untimed
+    e0.record()
+    for _ in range(k):
+        kg.nstream(A, B, C, scalar=3.0)
+    e1.record()
+    e1.synchronize()
+    t = e0.elapsed_time(e1) * 1e-3 / k
+    ar = length * sum(2.0 + 3.0 * 2.0 for _ in range(k + 1))
+    asum = float(A.abs().sum())
+    gbs = 32.0 * length / t / 1e9
+    print(json.dumps({"kernel": "nstream", "length": length, "iterations": k, "ms_per_iteration": round(t * 1e3, 4),
+                      "hbm_gbs": round(gbs, 1), "roofline_frac": round(gbs / peak_gbs(), 4),
+                      "validates": abs(ar - asum) / asum <= 1e-8}), flush=True)
+    del A, B, C
+    torch.cuda.empty_cache()
+    order = 16384
+    idx = torch.arange(order, dtype=torch.float64, device="cuda")
+    A = (order * idx[:, None] + idx[None, :]).contiguous()
+    B = torch.zeros((order, order), dtype=torch.float64, device="cuda")
+    kg.transpose(A, B)  # iteration 0, untimed
+    e0.record()
+    for _ in range(k):
+        kg.transpose(A, B)
+    e1.record()
+    e1.synchronize()
+    t = e0.elapsed_time(e1) * 1e-3 / k
+    ref = (order * idx[None, :] + idx[:, None]) * (1.0 + k) + (k + 1.0) * (k / 2.0)  # B[j][i] = (i*order+j)(K+1)+...
+    abserr = float((B - ref).abs().sum())
+    gbs = 32.0 * order * order / t / 1e9
+    print(json.dumps({"kernel": "transpose", "order": order, "iterations": k, "ms_per_iteration": round(t * 1e3, 4),
+                      "hbm_gbs": round(gbs, 1), "roofline_frac": round(gbs / peak_gbs(), 4),
+                      "abserr": abserr, "validates": abserr < 1e-8}), flush=True)
+
+
 def main() -> None:
     import torch
     ap = argparse.ArgumentParser()
-    ap.add_argument("which", choices=["sweep", "large", "batch"])
+    ap.add_argument("which", choices=["sweep", "large", "batch", "neighbours"])
     ap.add_argument("--depth", type=int, default=None)
     ap.add_argument("--grids", type=int, default=256)
     ap.add_argument("--n", type=int, default=None)
@@ -142,6 +188,8 @@ def main() -> None:
     elif args.which == "large":
         k = args.iterations or 200
         run_pair(torch, kg.STAR, 4, args.n or 46000, 65536, k)
+    elif args.which == "neighbours":
+        run_neighbours(torch, args.iterations or 20)
     else:
         run_batch(torch, args.iterations or 50, args.depth, args.grids)
 

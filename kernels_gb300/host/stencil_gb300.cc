@@ -48,13 +48,15 @@ int main(int argc, char* argv[])
 
     int iterations = 0, radius = 2;
     long long n = 0, tile_size = 32;
-    bool star = true, unfused = false, graph = false, json = false;
+    bool star = true, unfused = false, graph = false, json = false, tuned = false, whole = false;
     int dtype = PRK_FP64;
     int npos = 0;
     const char* pos[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     for (int a = 1; a < argc; ++a) {
         if (!std::strcmp(argv[a], "--unfused")) unfused = true;
         else if (!std::strcmp(argv[a], "--graph")) graph = true;
+        else if (!std::strcmp(argv[a], "--tuned")) tuned = true;
+        else if (!std::strcmp(argv[a], "--whole")) whole = true;
         else if (!std::strcmp(argv[a], "--json")) json = true;
         else if (!std::strcmp(argv[a], "--dtype") && a + 1 < argc) {
             const std::string d = argv[++a];
@@ -81,6 +83,7 @@ int main(int argc, char* argv[])
         if (npos > 4) radius = std::atoi(pos[4]);
         if (radius < 1 || 2LL * radius + 1 > n) throw "ERROR: Stencil radius negative or too large";
         if (unfused && dtype != PRK_FP64) throw "ERROR: --unfused drives the double-precision starR/gridR operators only";
+        if (unfused && (tuned || whole)) throw "ERROR: --tuned and --whole are fused forms";
     } catch (const char* e) {
         std::cout << e << std::endl;
         return 1;
@@ -100,7 +103,8 @@ int main(int argc, char* argv[])
     std::cout << "Radius of stencil    = " << radius << std::endl;
     std::cout << "Data type            = " << (dtype == PRK_FP64 ? "fp64" : "fp32c") << std::endl;
     std::cout << "Update form          = " << (unfused ? "unfused (stencil, then in += 1)" : "fused ping-pong")
-              << (graph ? ", CUDA graph" : "") << std::endl;
+              << (graph ? ", CUDA graph" : "") << (tuned ? ", tuned" : "")
+              << (whole ? ", whole run in one launch" : "") << std::endl;
 
     auto stencil = nothing;
     if (star) {
@@ -145,8 +149,9 @@ int main(int argc, char* argv[])
         stencil_time = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     } else {
         int final_in = 0;
-        if (prk_gb300_run(pattern, radius, n, dtype, iterations, d_in, d_in2, d_out, graph ? PRK_RUN_GRAPH : 0,
-                          &stencil_time, &final_in, nullptr) != PRK_OK)
+        const int flags = (graph ? PRK_RUN_GRAPH : 0) | (tuned ? PRK_RUN_TUNED : 0) | (whole ? PRK_RUN_WHOLE : 0);
+        if (prk_gb300_run(pattern, radius, n, dtype, iterations, d_in, d_in2, d_out, flags, &stencil_time, &final_in,
+                          nullptr) != PRK_OK)
             return die("run");
     }
 

@@ -69,6 +69,7 @@ def _cli(*args):
     ((10, 0), "ERROR: grid dimension must be positive"),
     ((10, 4, 32, "grid", 2), "ERROR: Stencil radius negative or too large"),
     ((10, 100, 32, "star", 0), "ERROR: Stencil radius negative or too large"),
+    ((10, 100, 32, "star", 2, "--unfused", "--whole"), "ERROR: --tuned and --whole are fused forms"),
 ])
 def test_cli_argument_errors_match_reference(args, msg):
     assert CLI.exists(), "stencil-gb300 was not built"

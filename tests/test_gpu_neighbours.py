@@ -1,0 +1,80 @@
+"""nstream and transpose on the GPU against the CPU restatement (oracle/prk_neighbours.py): bit for
+bit on random data, the reference's own validation on its initial data, ragged and unaligned
+sizes, and the argument checks."""
+import numpy as np
+import pytest
+
+import kernels_gb300 as kg
+from oracle import prk_neighbours as nb
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint64)
+
+
+@pytest.mark.parametrize("length", [1, 2, 3, 255, 1001, (1 << 20) + 3])
+@pytest.mark.parametrize("offsets", [(0, 0, 0), (1, 1, 1), (1, 0, 1), (0, 1, 0)])
+def test_nstream_bit_exact(cuda, length, offsets):
+    """Random values; A, B, C offset by one element each (16-byte vectors only when they share
+    their alignment)."""
+    rng = np.random.default_rng(length + 7 * sum(offsets))
+    a, b, c = (rng.standard_normal(length) * np.exp2(rng.integers(-20, 20, length)) for _ in range(3))
+    scalar = float(rng.standard_normal())
+    dev = []
+    for v, off in zip((a, b, c), offsets):
+        t = cuda.empty(length + 1, dtype=cuda.float64, device="cuda")
+        t[off:off + length] = cuda.from_numpy(v)
+        dev.append(t[off:off + length])
+    want = a.copy()
+    for _ in range(3):
+        kg.nstream(*dev, scalar=scalar)
+        nb.nstream(want, b, c, scalar)
+    assert np.array_equal(bits(dev[0].cpu().numpy()), bits(want))
+    assert np.array_equal(dev[1].cpu().numpy(), b) and np.array_equal(dev[2].cpu().numpy(), c)
+
+
+def test_nstream_reference_validation(cuda):
+    length, k = 10_000_019, 10
+    A = cuda.zeros(length, dtype=cuda.float64, device="cuda")
+    B = cuda.full((length,), 2.0, dtype=cuda.float64, device="cuda")
+    C = cuda.full((length,), 2.0, dtype=cuda.float64, device="cuda")
+    for _ in range(k + 1):
+        kg.nstream(A, B, C, scalar=3.0)
+    assert nb.nstream_validates(A.cpu().numpy(), k)
+
+
+@pytest.mark.parametrize("order", [1, 2, 3, 63, 64, 65, 129, 1000, 2048])
+def test_transpose_bit_exact(cuda, order):
+    rng = np.random.default_rng(order)
+    a = rng.standard_normal((order, order)) * np.exp2(rng.integers(-20, 20, (order, order)))
+    b = rng.standard_normal((order, order))
+    A, B = cuda.from_numpy(a.copy()).cuda(), cuda.from_numpy(b.copy()).cuda()
+    for _ in range(2):
+        kg.transpose(A, B)
+        nb.transpose(a, b)
+    assert np.array_equal(bits(A.cpu().numpy()), bits(a))
+    assert np.array_equal(bits(B.cpu().numpy()), bits(b))
+
+
+@pytest.mark.parametrize("order,k", [(1024, 10), (4096, 5), (999, 7)])
+def test_transpose_reference_validation(cuda, order, k):
+    a, b = nb.transpose_init(order)
+    A, B = cuda.from_numpy(a).cuda(), cuda.from_numpy(b).cuda()
+    for _ in range(k + 1):
+        kg.transpose(A, B)
+    assert nb.transpose_abserr(B.cpu().numpy(), k) < 1e-8
+    assert np.array_equal(A.cpu().numpy(), a + k + 1)
+
+
+def test_neighbour_rejections(cuda):
+    lib = kg.load()
+    A = cuda.zeros(1024, dtype=cuda.float64, device="cuda")
+    assert lib.prk_gb300_nstream(0, 3.0, A.data_ptr(), A.data_ptr(), A.data_ptr(), None) == -1
+    assert lib.prk_gb300_nstream(512, 3.0, A.data_ptr(), A[256:].data_ptr(), A[600:].data_ptr(), None) == -1  # A overlaps B
+    assert lib.prk_gb300_nstream(16, 3.0, None, A.data_ptr(), A.data_ptr(), None) == -1
+    M = cuda.zeros((32, 32), dtype=cuda.float64, device="cuda")
+    assert lib.prk_gb300_transpose(32, M.data_ptr(), M.data_ptr(), None) == -1  # A is B
+    assert lib.prk_gb300_transpose(0, M.data_ptr(), M.data_ptr(), None) == -1
+    assert lib.prk_gb300_transpose(1 << 23, M.data_ptr(), None, None) == -1

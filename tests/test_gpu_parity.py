@@ -172,7 +172,9 @@ def test_bounded_wait_reports_timeout_and_gpu_stays_usable(cuda):
 
 
 @pytest.mark.parametrize("args", [("10", "1000"), ("10", "200", "20", "grid", "3"), ("10", "200", "20", "star", "5", "--unfused"),
-                                  ("10", "1000", "32", "star", "2", "--dtype", "fp32c", "--graph")])
+                                  ("10", "1000", "32", "star", "2", "--dtype", "fp32c", "--graph"),
+                                  ("10", "1000", "32", "grid", "2", "--whole"), ("10", "1000", "32", "star", "2", "--tuned"),
+                                  ("10", "1000", "32", "star", "3", "--dtype", "fp32c", "--whole", "--graph")])
 def test_cli_driver_validates(cuda, args):
     """The C++ driver with the reference CLI prints the reference's verdict and rate lines."""
     import subprocess
