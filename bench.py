@@ -336,21 +336,28 @@ def run_gb300(args) -> None:
         # calls (re-zeroing out on the host) would time its wake-up. out accumulates instead: every
         # call adds 2(K+1) to each interior point, so its norm is known.
         kg.run_host(pattern, r, 1, h_in, h_out)
-        te, ev, norm_ok = 0.0, 0.0, True
+        te, ev, norm_ok, each = 0.0, 0.0, True, []
         for step in range(args.e2e_steps):
             barrier()
             t0 = time.perf_counter()
             res = kg.run_host(pattern, r, e2e_iters, h_in, h_out)
-            te += max_over_ranks(time.perf_counter() - t0)
+            each.append(max_over_ranks(time.perf_counter() - t0))
+            te += each[-1]
             ev += res["kernel_s"]
             norm_ok &= abs(res["norm"] - (4.0 + 2.0 * (e2e_iters + 1) * (step + 1))) <= 1e-8
         steps_e = args.e2e_steps
-        e2e = {"value": round(world * fl * (e2e_iters + 1) * steps_e / te / 1e9, 3), "unit": "GFLOP/s",
+        # The median call: the host link of a shared machine stalls now and then (one call in a few
+        # can take several times as long); every call's time and the mean are listed beside it.
+        t_med = sorted(each)[len(each) // 2]
+        e2e = {"value": round(world * fl * (e2e_iters + 1) / t_med / 1e9, 3), "unit": "GFLOP/s",
+               "statistic": "median of the timed calls",
+               "mean_value": round(world * fl * (e2e_iters + 1) * steps_e / te / 1e9, 3),
                "h2d_bytes_per_step": 2 * n * n * 8, "d2h_bytes_per_step": n * n * 8 + 8,
                "step": f"one prk_gb300_run_host call from pinned host buffers: in and out copied to the "
                        f"device in bands of rows, each band's {e2e_iters + 1} fused applications in one launch "
                        f"and its out copied back, overlapped across bands; device norm",
                "steps": steps_e, "seconds_per_step": round(te / steps_e, 4),
+               "seconds_each": [round(x, 4) for x in each],
                "evaluation_seconds_per_step": round(ev / steps_e, 4),
                "norm_ok": bool(norm_ok)}
 
@@ -411,7 +418,7 @@ def main() -> None:
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--radius", type=int, default=R_DEFAULT)
     ap.add_argument("--e2e-iterations", type=int, default=100)
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-applications", type=int, default=3)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")

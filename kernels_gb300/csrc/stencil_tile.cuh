@@ -370,11 +370,11 @@ __device__ __forceinline__ void fexact_points(const float* v, int ld, float (&S)
 }
 
 // fexact_points for the ROWS consecutive rows of a thread at once: S[rr] for the CPT points of row
-// r0 + rr, v pointing at V(r0, c0). Every row segment (star: every column strip) is read from
-// shared memory once and serves every row it is a tap of. The arithmetic is exact, so the order of
-// the terms does not matter.
+// r0 + rr, v pointing at V(r0, c0); own[rr] gets the values of those points. Every row segment
+// (star: every column strip) is read from shared memory once and serves every row it is a tap of.
+// The arithmetic is exact, so the order of the terms does not matter.
 template <int P, int R, int CPT, int ROWS, int RA>
-__device__ __forceinline__ void fexact_rows(const float* v, int ld, float (&S)[ROWS][CPT])
+__device__ __forceinline__ void fexact_rows(const float* v, int ld, float (&S)[ROWS][CPT], float (&own)[ROWS][CPT])
 {
     constexpr int SEG = CPT + 2 * RA;
     constexpr int NR = ROWS + 2 * R;  // rows r0 - R .. r0 + ROWS - 1 + R
@@ -390,6 +390,7 @@ __device__ __forceinline__ void fexact_rows(const float* v, int ld, float (&S)[R
 #pragma unroll
             for (int k = 0; k < CPT; ++k) {
                 col[rr + R][k] = m[k + RA];
+                own[rr][k] = m[k + RA];
                 S[rr][k] = 0.0f;
             }
 #pragma unroll
@@ -416,7 +417,10 @@ __device__ __forceinline__ void fexact_rows(const float* v, int ld, float (&S)[R
 #pragma unroll
         for (int rr = 0; rr < ROWS; ++rr) {
 #pragma unroll
-            for (int k = 0; k < CPT; ++k) S[rr][k] = 0.0f;
+            for (int k = 0; k < CPT; ++k) {
+                S[rr][k] = 0.0f;
+                own[rr][k] = seg[rr + R][k + RA];
+            }
 #pragma unroll
             for (int dr = 0; dr <= R; ++dr)
 #pragma unroll
@@ -501,21 +505,37 @@ __device__ __forceinline__ void advance_f32(float* p)
     }
 }
 
-// dst = src + 1 over the whole staged FP32 tile (the double-buffered FP32 route)
-template <int ELEMS>
-__device__ __forceinline__ void advance_f32_to(const float* src, float* dst)
+// dst = src + 1 over the halo of a staged FP32 tile only (the R rows above and below, the RA
+// columns either side): the interior points are advanced by the threads that own them. Rows as
+// 16-byte vectors, side columns as 8-byte pairs.
+template <int SW, int SH, int R, int RA>
+__device__ __forceinline__ void advance_halo_f32(const float* src, float* dst)
 {
-    constexpr int NV = ELEMS / 4;
+    static_assert(SW % 4 == 0 && RA % 2 == 0, "halo vectors");
+    constexpr int ROWV = SW / 4;               // 16-byte vectors in a row
+    constexpr int NROW = 2 * R * ROWV;         // top and bottom halo rows
+    constexpr int PER_SIDE = RA / 2;           // 8-byte pairs per side of a row
+    constexpr int NSIDE = (SH - 2 * R) * 2 * PER_SIDE;
 #pragma unroll
-    for (int q = 0; q < (NV + THREADS - 1) / THREADS; ++q) {
-        const int idx = threadIdx.x + q * THREADS;
-        if (NV % THREADS == 0 || idx < NV) {
-            float4 v = reinterpret_cast<const float4*>(src)[idx];
-            v.x = __fadd_rn(v.x, 1.0f);
-            v.y = __fadd_rn(v.y, 1.0f);
-            v.z = __fadd_rn(v.z, 1.0f);
-            v.w = __fadd_rn(v.w, 1.0f);
-            reinterpret_cast<float4*>(dst)[idx] = v;
+    for (int q = 0; q < (NROW + NSIDE + THREADS - 1) / THREADS; ++q) {
+        const int h = threadIdx.x + q * THREADS;
+        if (h < NROW) {
+            const int r = h / ROWV, v = h - r * ROWV;
+            const int row = r < R ? r : SH - 2 * R + r;  // rows 0..R-1, then SH-R..SH-1
+            float4 x = reinterpret_cast<const float4*>(src + row * SW)[v];
+            x.x = __fadd_rn(x.x, 1.0f);
+            x.y = __fadd_rn(x.y, 1.0f);
+            x.z = __fadd_rn(x.z, 1.0f);
+            x.w = __fadd_rn(x.w, 1.0f);
+            reinterpret_cast<float4*>(dst + row * SW)[v] = x;
+        } else if (h < NROW + NSIDE) {
+            const int i = h - NROW;
+            const int row = R + i / (2 * PER_SIDE), p = i - (i / (2 * PER_SIDE)) * (2 * PER_SIDE);
+            const int col = p < PER_SIDE ? 2 * p : SW - RA + 2 * (p - PER_SIDE);
+            float2 x = *reinterpret_cast<const float2*>(src + row * SW + col);
+            x.x = __fadd_rn(x.x, 1.0f);
+            x.y = __fadd_rn(x.y, 1.0f);
+            *reinterpret_cast<float2*>(dst + row * SW + col) = x;
         }
     }
 }
@@ -858,18 +878,26 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
             // The same applications in their tightest form: the route is fixed for the launch, and
             // a thread's S for all its rows comes from one pass over its column strip. The FP32
             // tile takes half of the binary64 stage, so the other half holds the next
-            // application's in: while application t reads one, in + 1 is written to the other, and
-            // one barrier per application separates them.
+            // application's in: while application t reads one, in + 1 is written to the other (each
+            // thread its own points, from the values it has just read, and the threads together
+            // the halo), and one barrier per application separates them.
             if constexpr (EXACT) {
                 float* const buf = reinterpret_cast<float*>(s_in);
                 const int own = (warp * ROWS + R) * G::SW + G::RA + c0;
 #pragma unroll 1
                 for (int t = 0; t < nsteps; ++t) {
                     const int cur = (t & 1) * G::ELEMS;
-                    float S[ROWS][CPT];
-                    fexact_rows<P, R, CPT, ROWS, G::RA>(buf + cur + own, G::SW, S);
+                    float S[ROWS][CPT], v[ROWS][CPT];
+                    fexact_rows<P, R, CPT, ROWS, G::RA>(buf + cur + own, G::SW, S, v);
                     if (t + 1 < nsteps) {
-                        advance_f32_to<G::ELEMS>(buf + cur, buf + (G::ELEMS - cur));
+                        float* nx = buf + (G::ELEMS - cur);
+#pragma unroll
+                        for (int rr = 0; rr < ROWS; ++rr) {
+                            static_assert(CPT == 2, "own points move as one 8-byte pair");
+                            *reinterpret_cast<float2*>(nx + own + rr * G::SW) =
+                                make_float2(__fadd_rn(v[rr][0], 1.0f), __fadd_rn(v[rr][1], 1.0f));
+                        }
+                        advance_halo_f32<G::SW, G::SH, R, G::RA>(buf + cur, nx);
                         __syncthreads();
                     }
 #pragma unroll
