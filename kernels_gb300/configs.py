@@ -9,8 +9,8 @@ case. The cases are seeded synthetic PRK fields (in = i+j, out = 0), the same sh
   large   star R=4, FP32C at n = 65536 and FP64 at n = 46000, 200 iterations, tuned depth
   batch   the seeded 256-grid batch (kernels_gb300.workloads), FP64 and FP32C, one CUDA graph, tuned
           depth per grid (or --depth D for every grid)
-  neighbours  nstream (length 2^28, the reference's A = 0, B = C = 2, scalar 3) and transpose
-          (order 16384, A[j][i] = order*j + i, B = 0), 20 timed iterations after one untimed:
+  neighbours  nstream (length n*n = 2^28, the reference's A = 0, B = C = 2, scalar 3) and transpose
+          (order n = 16384, A[j][i] = order*j + i, B = 0), 20 timed iterations after one untimed:
           HBM GB/s as the reference rates them (32 B per element and iteration for both) and its
           fraction of the measured peak; validation by the reference's own formulas, on the GPU
 
@@ -126,10 +126,10 @@ def run_batch(torch, iterations: int, depth: int | None, count: int):
         torch.cuda.empty_cache()
 
 
-def run_neighbours(torch, iterations: int) -> None:
-    """nstream and transpose timed with CUDA events; validated on the device."""
+def run_neighbours(torch, iterations: int, n: int) -> None:
+    """nstream (length n*n) and transpose (order n) timed with CUDA events; validated on the device."""
     k = iterations
-    length = 1 << 28
+    length = n * n
     A = torch.zeros(length, dtype=torch.float64, device="cuda")
     B = torch.full((length,), 2.0, dtype=torch.float64, device="cuda")
     C = torch.full((length,), 2.0, dtype=torch.float64, device="cuda")
@@ -149,7 +149,7 @@ def run_neighbours(torch, iterations: int) -> None:
                       "validates": abs(ar - asum) / asum <= 1e-8}), flush=True)
     del A, B, C
     torch.cuda.empty_cache()
-    order = 16384
+    order = n
     idx = torch.arange(order, dtype=torch.float64, device="cuda")
     A = (order * idx[:, None] + idx[None, :]).contiguous()
     B = torch.zeros((order, order), dtype=torch.float64, device="cuda")
@@ -189,7 +189,7 @@ def main() -> None:
         k = args.iterations or 200
         run_pair(torch, kg.STAR, 4, args.n or 46000, 65536, k)
     elif args.which == "neighbours":
-        run_neighbours(torch, args.iterations or 20)
+        run_neighbours(torch, args.iterations or 20, args.n or 16384)
     else:
         run_batch(torch, args.iterations or 50, args.depth, args.grids)
 

@@ -35,6 +35,48 @@ def test_nstream_bit_exact(cuda, length, offsets):
     assert np.array_equal(dev[1].cpu().numpy(), b) and np.array_equal(dev[2].cpu().numpy(), c)
 
 
+def _mixed(rng, n, bound):
+    """Whole numbers up to about `bound` (both signs, both zeros) mixed with fractional values."""
+    v = rng.integers(-bound, bound, n).astype(np.float64)
+    v[rng.random(n) < 0.05] = 0.0
+    v[rng.random(n) < 0.05] = -0.0
+    frac = rng.random(n) < 0.1
+    v[frac] += 0.5
+    v[rng.random(n) < 0.02] = 2.0 ** 20  # just above the certified bound
+    return v
+
+
+@pytest.mark.parametrize("scalar", [3.0, -7.0, 0.0, -0.0, 8.0, 9.0, 2.5])
+def test_nstream_exact_route_bit_exact(cuda, scalar):
+    """Whole-number data near the certified bounds, mixed in a warp with values outside them; whole
+    and non-whole scalars."""
+    n = (1 << 16) + 5
+    rng = np.random.default_rng(int(abs(scalar) * 10) + 3)
+    a, b, c = (_mixed(rng, n, 2 ** 19) for _ in range(3))
+    A, B, C_ = (cuda.from_numpy(x.copy()).cuda() for x in (a, b, c))
+    want = a.copy()
+    for _ in range(3):
+        kg.nstream(A, B, C_, scalar=scalar)
+        nb.nstream(want, b, c, scalar)
+    assert np.array_equal(bits(A.cpu().numpy()), bits(want))
+
+
+def test_transpose_exact_route_bit_exact(cuda):
+    order = 777
+    rng = np.random.default_rng(11)
+    a = _mixed(rng, order * order, 2 ** 50).reshape(order, order)
+    b = _mixed(rng, order * order, 2 ** 50).reshape(order, order)
+    # A += 1 edges: 2^k - 1 (the carry steps the exponent), powers of two, 2^53 and above, negatives
+    edges = [2.0 ** k - 1 for k in range(1, 54)] + [2.0 ** k for k in range(0, 55)] + [-1.0, -2.0 ** 40, -3.5]
+    a.flat[:len(edges)] = edges
+    A, B = cuda.from_numpy(a.copy()).cuda(), cuda.from_numpy(b.copy()).cuda()
+    for _ in range(3):
+        kg.transpose(A, B)
+        nb.transpose(a, b)
+    assert np.array_equal(bits(A.cpu().numpy()), bits(a))
+    assert np.array_equal(bits(B.cpu().numpy()), bits(b))
+
+
 def test_nstream_reference_validation(cuda):
     length, k = 10_000_019, 10
     A = cuda.zeros(length, dtype=cuda.float64, device="cuda")
