@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(GEN_THREADS)
         const T* sp = s + (r + R) * SW + (c + R);
         if (in_next) {
             if constexpr (DT == FP64)
-                in_next[gi * n + gj] = __dadd_rn(*sp, 1.0);
+                in_next[gi * n + gj] = inc_exact(*sp);
             else
                 in_next[gi * n + gj] = __fadd_rn(*sp, 1.0f);
         }
@@ -97,7 +97,7 @@ __global__ void k_add(int64_t total, void* in_v)
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     for (int64_t k = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < total; k += stride) {
         if constexpr (DT == FP64)
-            in[k] = __dadd_rn(in[k], 1.0);
+            in[k] = inc_exact(in[k]);
         else
             in[k] = __fadd_rn(in[k], 1.0f);
     }

@@ -3,8 +3,8 @@
 // call, as the reference's timed loop makes it; binary64 with every product and sum rounded on its
 // own, in the reference's order, so the results are those of its strict evaluation.
 //
-// transpose's A += 1 has an exact integer form for positive whole numbers (inc below); B += A^T
-// stays a binary64 add.
+// transpose's A += 1 has an exact integer form for positive whole numbers (inc_exact,
+// prk_arith.cuh); B += A^T stays a binary64 add.
 //
 // nstream's three binary64 operations per element keep this GPU's binary64 pipe 82% busy at 68% of
 // DRAM peak, so it has a certified exact route: where the operands are whole numbers below 2^20
@@ -26,6 +26,7 @@
 #include <cstdint>
 
 #include "../../include/prk_gb300.h"
+#include "prk_arith.cuh"
 #include "prk_internal.cuh"
 
 namespace prk {
@@ -110,21 +111,6 @@ __global__ void __launch_bounds__(NS_THREADS) k_nstream(int64_t head, int64_t nv
     }
 }
 
-// a + 1 for transpose's A. For a positive whole number 1 <= a < 2^53 the sum is exact, and its
-// encoding is a's plus one unit of the integer position: the mantissa field's 2^(1075 - e) bit,
-// whose carry steps the exponent when the mantissa overflows (a = 2^k - 1). Anything else takes
-// the binary64 add.
-__device__ __forceinline__ double inc(double a)
-{
-    const uint64_t b = static_cast<uint64_t>(__double_as_longlong(a));
-    const int e = static_cast<int>(b >> 52);  // the sign bit makes e >= 2048 for negative a
-    if (e >= 1023 && e <= 1075) {
-        const uint64_t unit = 1ull << (1075 - e);
-        if ((b & (unit - 1)) == 0) return __longlong_as_double(static_cast<long long>(b + unit));
-    }
-    return __dadd_rn(a, 1.0);
-}
-
 constexpr int TT = 64;           // transpose tile edge
 constexpr int TP = TT + 1;       // padded row length of the shared tile
 constexpr int TR_THREADS = 256;  // 8 warps
@@ -174,10 +160,10 @@ __global__ void __launch_bounds__(TR_THREADS, 2) k_transpose(int64_t order, doub
         if (y < order) {
             double* p = A + y * order + x;
             if (vec && x + 1 < order) {
-                *reinterpret_cast<double2*>(p) = make_double2(inc(a0[q]), inc(a1[q]));
+                *reinterpret_cast<double2*>(p) = make_double2(inc_exact(a0[q]), inc_exact(a1[q]));
             } else {
-                if (x < order) p[0] = inc(a0[q]);
-                if (x + 1 < order) p[1] = inc(a1[q]);
+                if (x < order) p[0] = inc_exact(a0[q]);
+                if (x + 1 < order) p[1] = inc_exact(a1[q]);
             }
         }
     }

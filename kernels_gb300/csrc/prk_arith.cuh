@@ -101,6 +101,21 @@ __device__ __forceinline__ void fp32c_point(const float* s, int ld, float& s_hi,
     s_lo = lo;
 }
 
+// fl(a + 1) without the binary64 pipe where that is exact: for a positive whole number
+// 1 <= a < 2^53 the sum's encoding is a's plus one unit of the integer position (the mantissa's
+// 2^(1075 - e) bit; its carry steps the exponent when the mantissa overflows). Other values take
+// the binary64 add.
+__device__ __forceinline__ double inc_exact(double a)
+{
+    const uint64_t b = static_cast<uint64_t>(__double_as_longlong(a));
+    const int e = static_cast<int>(b >> 52);  // >= 2048 for negative a
+    if (e >= 1023 && e <= 1075) {
+        const uint64_t unit = 1ull << (1075 - e);
+        if ((b & (unit - 1)) == 0) return __longlong_as_double(static_cast<long long>(b + unit));
+    }
+    return __dadd_rn(a, 1.0);
+}
+
 // (o_hi, o_lo) += (s_hi, s_lo), renormalised so that |o_lo| <= ulp(o_hi)/2.
 __device__ __forceinline__ void df_add(float& o_hi, float& o_lo, float s_hi, float s_lo)
 {

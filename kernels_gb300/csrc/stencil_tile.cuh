@@ -565,8 +565,8 @@ __device__ __forceinline__ void advance_f64(double* p)
         const int idx = threadIdx.x + q * THREADS;
         if (NV % THREADS == 0 || idx < NV) {
             double2 v = reinterpret_cast<double2*>(p)[idx];
-            v.x = __dadd_rn(v.x, 1.0);
-            v.y = __dadd_rn(v.y, 1.0);
+            v.x = inc_exact(v.x);
+            v.y = inc_exact(v.y);
             reinterpret_cast<double2*>(p)[idx] = v;
         }
     }
@@ -783,7 +783,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
 #pragma unroll
             for (int k = 0; k < CPT; ++k) {
                 if constexpr (DT == FP64)
-                    nxt[k] = __dadd_rn(s_in[soff + k], 1.0);
+                    nxt[k] = inc_exact(s_in[soff + k]);
                 else
                     nxt[k] = __fadd_rn(s_in[soff + k], 1.0f);
             }
