@@ -100,6 +100,77 @@ PRK_HD uint64_t from_fixed(int64_t x, int unit)
     return s | ((static_cast<uint64_t>(msb + unit + 1022) << 52) + m);
 }
 
+// Bits of fl(w * v), the binary64 product rounded to nearest-even, for a normal binary64 w (encoding
+// wb, biased exponent at most 2014) and a whole number |v| < 2^31, from integer multiplies on w's
+// 53-bit significand: W * |v| < 2^84 as two 64-bit words, its top 53 bits rounded on the bits
+// below (the half-way case to the even neighbour). v = 0 gives the zero of w's sign (w * +0).
+PRK_HD uint64_t mul_whole(uint64_t wb, int32_t v)
+{
+    if (v == 0) return wb & SIGN;
+    const uint64_t sign = (wb & SIGN) ^ (v < 0 ? SIGN : 0);
+    const uint64_t a = v < 0 ? static_cast<uint64_t>(-static_cast<int64_t>(v)) : static_cast<uint64_t>(v);
+    const int ew = static_cast<int>((wb >> 52) & 0x7FF);
+    const uint64_t W = (wb & MANT) | HIDDEN;                 // 2^52 <= W < 2^53
+    const uint64_t pl = (W & 0xFFFFFFFFull) * a;             // < 2^63
+    const uint64_t ph = (W >> 32) * a;                       // < 2^52
+    const uint64_t lo = pl + (ph << 32);                     // W * a = hi * 2^64 + lo
+    const uint64_t hi = (ph >> 32) + (lo < pl ? 1u : 0u);
+    const int len = hi ? 128 - clz64(hi) : 64 - clz64(lo);   // bit length of W * a, 53..84
+    const int sh = len - 53;                                 // bits rounded away, 0..31
+    uint64_t q = lo, rem = 0, half = 0;
+    if (sh > 0) {
+        q = (lo >> sh) | (hi << (64 - sh));
+        rem = lo & ((1ull << sh) - 1);
+        half = 1ull << (sh - 1);
+    }
+    int e = ew + sh;  // W * a = q * 2^sh, and q in [2^52, 2^53) makes the biased exponent ew + sh
+    if (sh > 0 && (rem > half || (rem == half && (q & 1)))) {
+        ++q;
+        if (q >> 53) {
+            q >>= 1;
+            ++e;
+        }
+    }
+    return sign | (static_cast<uint64_t>(e) << 52) | (q & MANT);
+}
+
+PRK_HD int clz32(uint32_t x)
+{
+#ifdef __CUDA_ARCH__
+    return __clz(static_cast<int>(x));
+#else
+    return x ? __builtin_clz(x) : 32;
+#endif
+}
+
+// mul_whole for |v| < 2^20 in 32-bit words (w's biased exponent at most 2025): W * |v| < 2^73 is
+// formed as three words from two 32 x 32 -> 64-bit products, and its top 53 bits are taken with
+// two 64-bit funnel shifts. The same bits as mul_whole and as the binary64 multiply.
+PRK_HD uint64_t mul_whole20(uint64_t wb, int32_t v)
+{
+    const uint32_t whi = static_cast<uint32_t>(wb >> 32);
+    if (v == 0) return static_cast<uint64_t>(whi & 0x80000000u) << 32;
+    const uint32_t sign = (whi ^ (v < 0 ? 0x80000000u : 0u)) & 0x80000000u;
+    const uint32_t a = static_cast<uint32_t>(v < 0 ? -v : v);
+    const uint64_t x = static_cast<uint64_t>(static_cast<uint32_t>(wb)) * a;  // low word of W times a, < 2^52
+    const uint64_t y = static_cast<uint64_t>((whi & 0xFFFFFu) | 0x100000u) * a;  // high 21 bits, < 2^41
+    const uint64_t mid = (x >> 32) + (y & 0xFFFFFFFFull);
+    const uint32_t p0 = static_cast<uint32_t>(x), p1 = static_cast<uint32_t>(mid);
+    const uint32_t p2 = static_cast<uint32_t>((y >> 32) + (mid >> 32));  // W * a = p2:p1:p0, p2 < 2^9
+    const int sh = (p2 ? 96 - clz32(p2) : 64 - clz32(p1)) - 53;          // bits rounded away, 0..20
+    const uint32_t q_lo = static_cast<uint32_t>(((static_cast<uint64_t>(p1) << 32) | p0) >> sh);
+    const uint32_t q_hi = static_cast<uint32_t>(((static_cast<uint64_t>(p2) << 32) | p1) >> sh);
+    const uint32_t mask = (1u << sh) - 1u, rem = p0 & mask, half = (mask >> 1) + (sh > 0 ? 1u : 0u);
+    const bool up = sh > 0 && (rem > half || (rem == half && (q_lo & 1u)));
+    uint64_t q = ((static_cast<uint64_t>(q_hi) << 32) | q_lo) + (up ? 1u : 0u);
+    uint32_t e = ((whi >> 20) & 0x7FFu) + static_cast<uint32_t>(sh);
+    if (q >> 53) {
+        q >>= 1;
+        ++e;
+    }
+    return (static_cast<uint64_t>(sign | (e << 20)) << 32) | (q & MANT);
+}
+
 // Certification of a tile whose values have lowest-bit exponents >= lo_min and highest-bit
 // exponents <= hi_max, for a stencil with weight shift `shift` and coefficient L1 norm `coef_l1`
 // (sum |w| * 2^shift), and `steps` in += 1 updates applied to the tile before its last use.

@@ -572,6 +572,105 @@ __device__ __forceinline__ void advance_f64(double* p)
     }
 }
 
+// binary64 encoding of a constexpr double (normal or zero), by exact scaling by powers of two
+// (C++17 has no bit_cast in constant expressions).
+__host__ __device__ constexpr uint64_t encode(double w)
+{
+    if (w == 0.0) return 0;
+    uint64_t sign = 0;
+    if (w < 0) {
+        sign = fx::SIGN;
+        w = -w;
+    }
+    int e = 0;
+    while (w >= 2.0) {
+        w /= 2.0;
+        ++e;
+    }
+    while (w < 1.0) {
+        w *= 2.0;
+        --e;
+    }
+    const uint64_t frac = static_cast<uint64_t>((w - 1.0) * 4503599627370496.0);  // exact: 52 bits
+    return sign | (static_cast<uint64_t>(e + 1023) << 52) | frac;
+}
+static_assert(encode(1.0) == 0x3FF0000000000000ull && encode(-0.125) == 0xBFC0000000000000ull &&
+                  encode(1.0 / 6.0) == 0x3FC5555555555555ull,
+              "constexpr binary64 encoding");
+
+// The taps of a stencil in the generator's order (column offset outer, row offset inner, zero
+// weights left out), with their offsets in a tile of row length LD and their weights' encodings.
+template <int P, int R, int LD>
+struct TapTable {
+    struct Tap {
+        int off;
+        int pad;
+        uint64_t wb;
+    } tap[tap_count(P, R)];
+};
+
+template <int P, int R, int LD>
+constexpr TapTable<P, R, LD> make_taps()
+{
+    TapTable<P, R, LD> t{};
+    int k = 0;
+    for (int dc = -R; dc <= R; ++dc)
+        for (int dr = -R; dr <= R; ++dr) {
+            const double w = weight(P, R, dc, dr);
+            if (w != 0.0) {
+                t.tap[k].off = dr * LD + dc;
+                t.tap[k].pad = 0;
+                t.tap[k].wb = encode(w);
+                ++k;
+            }
+        }
+    return t;
+}
+
+template <int P, int R, int LD>
+__constant__ TapTable<P, R, LD> c_taps = make_taps<P, R, LD>();
+
+// fp64_point for CPT adjacent points of a tile of whole numbers |v| < 2^20 held as int32: every
+// product comes from fx::mul_whole20 on the integer pipes (the same bits as __dmul_rn), every sum is
+// the same binary64 add in the same order, so the binary64 pipe issues one instruction per tap
+// instead of two. The taps come from constant memory in a loop, which keeps the code small.
+template <int P, int R, int LD, int CPT>
+__device__ __forceinline__ void fp64_points_whole(const int32_t* s, double (&acc)[CPT])
+{
+    constexpr int N = tap_count(P, R);
+    const auto& T = c_taps<P, R, LD>;
+#pragma unroll
+    for (int k = 0; k < CPT; ++k)
+        acc[k] = __longlong_as_double(static_cast<long long>(fx::mul_whole20(T.tap[0].wb, s[T.tap[0].off + k])));
+#pragma unroll 2
+    for (int t = 1; t < N; ++t) {
+        const int off = T.tap[t].off;
+        const uint64_t wb = T.tap[t].wb;
+#pragma unroll
+        for (int k = 0; k < CPT; ++k)
+            acc[k] = __dadd_rn(acc[k], __longlong_as_double(static_cast<long long>(fx::mul_whole20(wb, s[off + k]))));
+    }
+}
+
+// in += 1 over a staged tile of int32 whole numbers, as 16-byte vectors.
+template <int ELEMS>
+__device__ __forceinline__ void advance_i32(int32_t* p)
+{
+    constexpr int NV = ELEMS / 4;
+#pragma unroll
+    for (int q = 0; q < (NV + THREADS - 1) / THREADS; ++q) {
+        const int idx = threadIdx.x + q * THREADS;
+        if (NV % THREADS == 0 || idx < NV) {
+            int4 v = reinterpret_cast<int4*>(p)[idx];
+            v.x += 1;
+            v.y += 1;
+            v.z += 1;
+            v.w += 1;
+            reinterpret_cast<int4*>(p)[idx] = v;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------------------------
 // The kernel
 
@@ -688,6 +787,39 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
         }
         __syncthreads();  // every converted word visible
     }
+    // ---- FP64, other weights: whole-number tiles take their products off the binary64 pipe ----
+    // Every value +0 or a whole number below 2^19 (so that up to 2^19 applications of in += 1 stay
+    // below 2^20): the tile is held as int32 and fp64_points_whole evaluates it.
+    bool iwhole = false;
+    if constexpr (DT == FP64 && !EXACT) {
+        constexpr int PER = (G::ELEMS + THREADS - 1) / THREADS;
+        const uint64_t* raw = reinterpret_cast<const uint64_t*>(s_in);
+        int32_t iv[PER];
+        bool ok = nsteps <= (1 << 19);
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int idx = threadIdx.x + q * THREADS;
+            const uint64_t b = idx < G::ELEMS ? raw[idx] : 0ull;
+            const int e = static_cast<int>((b >> 52) & 0x7FF);
+            const int sh = 1075 - e;  // fraction bits below the binary point, 34..52 in range
+            const bool in_range = e >= 1023 && e <= 1041;
+            const uint64_t m = (b & fx::MANT) | fx::HIDDEN;
+            const bool whole = in_range && (m & ((1ull << (sh & 63)) - 1)) == 0;
+            const int32_t a = in_range ? static_cast<int32_t>(m >> (sh & 63)) : 0;
+            iv[q] = b == 0ull ? 0 : ((b >> 63) ? -a : a);
+            ok = ok && (b == 0ull || whole);
+        }
+        iwhole = __syncthreads_and(ok) != 0;
+        if (iwhole) {
+            int32_t* si = reinterpret_cast<int32_t*>(s_in);
+#pragma unroll
+            for (int q = 0; q < PER; ++q) {
+                const int idx = threadIdx.x + q * THREADS;
+                if (idx < G::ELEMS) si[idx] = iv[q];
+            }
+        }
+        __syncthreads();
+    }
 
     // Set by the multi-application FP32 route when the tile's out words are held as integers
     bool oint = false;
@@ -735,6 +867,15 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
                     done = true;
                 }
             }
+            if constexpr (!EXACT) {
+                if (iwhole) {
+                    double S[CPT];
+                    fp64_points_whole<P, R, G::SW, CPT>(reinterpret_cast<const int32_t*>(s_in) + soff, S);
+#pragma unroll
+                    for (int k = 0; k < CPT; ++k) o[k] = as_bits(__dadd_rn(as_dbl(o[k]), S[k]));
+                    done = true;
+                }
+            }
             if (!done) {
                 const double* sp = reinterpret_cast<const double*>(s_in) + soff;
 #pragma unroll
@@ -776,6 +917,14 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
 #pragma unroll
                     for (int k = 0; k < CPT; ++k) nxt[k] = as_dbl(fx::from_fixed(v[k] + one, unit));
                 }
+                done = true;
+            }
+        }
+        if constexpr (DT == FP64 && !EXACT) {
+            if (iwhole) {
+                const int32_t* v = reinterpret_cast<const int32_t*>(s_in) + soff;
+#pragma unroll
+                for (int k = 0; k < CPT; ++k) nxt[k] = as_dbl(from_fixed32(v[k] + 1, 0));
                 done = true;
             }
         }
@@ -926,6 +1075,12 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
                             adv = true;
                         } else if (unit != fx::NOT_FIXED) {
                             advance_i64<G::ELEMS>(reinterpret_cast<int64_t*>(s_in), 1ll << (-unit));
+                            adv = true;
+                        }
+                    }
+                    if constexpr (!EXACT) {
+                        if (iwhole) {
+                            advance_i32<G::ELEMS>(reinterpret_cast<int32_t*>(s_in));
                             adv = true;
                         }
                     }

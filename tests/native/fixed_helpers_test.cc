@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstring>
 #include <random>
+#include <vector>
 
 #include "prk_fixed.cuh"
 
@@ -63,6 +64,48 @@ int main()
     bad += certify(0, 50, 3, 12, 1) != NOT_FIXED;
     bad += certify(NOT_FIXED, 3, 3, 12, 1) != NOT_FIXED;
     bad += certify(ZERO_LO, ZERO_HI, 3, 12, 1) != 0;
+    // mul_whole against the host's binary64 multiply: the stencil weights and random normal w,
+    // random and edge whole numbers v with |v| < 2^31
+    {
+        std::vector<double> ws;
+        for (int R = 1; R <= 5; ++R)
+            for (int j = 1; j <= R; ++j) {
+                ws.push_back(1.0 / (2.0 * j * R));
+                ws.push_back(-1.0 / (2.0 * j * R));
+                ws.push_back(1.0 / (4.0 * j * (2.0 * j - 1) * R));
+                ws.push_back(-1.0 / (4.0 * j * R));
+            }
+        for (int t = 0; t < 2000; ++t) {
+            double w = std::ldexp(1.0 + static_cast<double>(g() >> 12) * 0x1p-52, static_cast<int>(g() % 200) - 100);
+            ws.push_back(g() & 1 ? -w : w);
+        }
+        std::vector<int32_t> vs = {0, 1, -1, 2, 3, 7, 2147483647, -2147483647};
+        for (int k = 1; k < 31; ++k) {
+            vs.push_back((1 << k) - 1);
+            vs.push_back(1 << k);
+            vs.push_back(-(1 << k) + 1);
+            vs.push_back((1 << k) + 1);
+        }
+        for (int t = 0; t < 3000; ++t) {
+            const int32_t v = static_cast<int32_t>(g() >> (33 + g() % 31));
+            vs.push_back(g() & 1 ? -v : v);
+        }
+        long checked = 0;
+        for (double w : ws)
+            for (int32_t v : vs) {
+                const double want = w * static_cast<double>(v);
+                bad += mul_whole(bits(w), v) != bits(want);
+                if (v > -(1 << 20) && v < (1 << 20)) bad += mul_whole20(bits(w), v) != bits(want);
+                ++checked;
+            }
+        // every |v| < 2^20 against a few weights
+        for (double w : {1.0 / 6.0, -1.0 / 18.0, 1.0 / 48.0, -1.0 / 100.0, 1.0 / 30.0})
+            for (int32_t v = -(1 << 20) + 1; v < (1 << 20); ++v) {
+                bad += mul_whole20(bits(w), v) != bits(w * static_cast<double>(v));
+                ++checked;
+            }
+        std::printf("mul_whole checked=%ld\n", checked);
+    }
     std::printf("bad=%d\n", bad);
     return bad != 0;
 }
