@@ -100,40 +100,6 @@ PRK_HD uint64_t from_fixed(int64_t x, int unit)
     return s | ((static_cast<uint64_t>(msb + unit + 1022) << 52) + m);
 }
 
-// Bits of fl(w * v), the binary64 product rounded to nearest-even, for a normal binary64 w (encoding
-// wb, biased exponent at most 2014) and a whole number |v| < 2^31, from integer multiplies on w's
-// 53-bit significand: W * |v| < 2^84 as two 64-bit words, its top 53 bits rounded on the bits
-// below (the half-way case to the even neighbour). v = 0 gives the zero of w's sign (w * +0).
-PRK_HD uint64_t mul_whole(uint64_t wb, int32_t v)
-{
-    if (v == 0) return wb & SIGN;
-    const uint64_t sign = (wb & SIGN) ^ (v < 0 ? SIGN : 0);
-    const uint64_t a = v < 0 ? static_cast<uint64_t>(-static_cast<int64_t>(v)) : static_cast<uint64_t>(v);
-    const int ew = static_cast<int>((wb >> 52) & 0x7FF);
-    const uint64_t W = (wb & MANT) | HIDDEN;                 // 2^52 <= W < 2^53
-    const uint64_t pl = (W & 0xFFFFFFFFull) * a;             // < 2^63
-    const uint64_t ph = (W >> 32) * a;                       // < 2^52
-    const uint64_t lo = pl + (ph << 32);                     // W * a = hi * 2^64 + lo
-    const uint64_t hi = (ph >> 32) + (lo < pl ? 1u : 0u);
-    const int len = hi ? 128 - clz64(hi) : 64 - clz64(lo);   // bit length of W * a, 53..84
-    const int sh = len - 53;                                 // bits rounded away, 0..31
-    uint64_t q = lo, rem = 0, half = 0;
-    if (sh > 0) {
-        q = (lo >> sh) | (hi << (64 - sh));
-        rem = lo & ((1ull << sh) - 1);
-        half = 1ull << (sh - 1);
-    }
-    int e = ew + sh;  // W * a = q * 2^sh, and q in [2^52, 2^53) makes the biased exponent ew + sh
-    if (sh > 0 && (rem > half || (rem == half && (q & 1)))) {
-        ++q;
-        if (q >> 53) {
-            q >>= 1;
-            ++e;
-        }
-    }
-    return sign | (static_cast<uint64_t>(e) << 52) | (q & MANT);
-}
-
 PRK_HD int clz32(uint32_t x)
 {
 #ifdef __CUDA_ARCH__
@@ -143,9 +109,11 @@ PRK_HD int clz32(uint32_t x)
 #endif
 }
 
-// mul_whole for |v| < 2^20 in 32-bit words (w's biased exponent at most 2025): W * |v| < 2^73 is
-// formed as three words from two 32 x 32 -> 64-bit products, and its top 53 bits are taken with
-// two 64-bit funnel shifts. The same bits as mul_whole and as the binary64 multiply.
+// Bits of fl(w * v), the binary64 product rounded to nearest-even, for a normal binary64 w (encoding
+// wb, biased exponent at most 2025) and a whole number |v| < 2^20, from integer operations on w's
+// 53-bit significand W: W * |v| < 2^73 is formed as three 32-bit words from two 32 x 32 -> 64-bit
+// products, its top 53 bits are taken with two 64-bit funnel shifts and rounded on the bits below
+// (the half-way case to the even neighbour). v = 0 gives the zero of w's sign (w * +0).
 PRK_HD uint64_t mul_whole20(uint64_t wb, int32_t v)
 {
     const uint32_t whi = static_cast<uint32_t>(wb >> 32);

@@ -64,8 +64,8 @@ int main()
     bad += certify(0, 50, 3, 12, 1) != NOT_FIXED;
     bad += certify(NOT_FIXED, 3, 3, 12, 1) != NOT_FIXED;
     bad += certify(ZERO_LO, ZERO_HI, 3, 12, 1) != 0;
-    // mul_whole against the host's binary64 multiply: the stencil weights and random normal w,
-    // random and edge whole numbers v with |v| < 2^31
+    // mul_whole20 against the host's binary64 multiply: the stencil weights and random normal w,
+    // random and edge whole numbers v with |v| < 2^20
     {
         std::vector<double> ws;
         for (int R = 1; R <= 5; ++R)
@@ -94,8 +94,8 @@ int main()
         for (double w : ws)
             for (int32_t v : vs) {
                 const double want = w * static_cast<double>(v);
-                bad += mul_whole(bits(w), v) != bits(want);
-                if (v > -(1 << 20) && v < (1 << 20)) bad += mul_whole20(bits(w), v) != bits(want);
+                if (v <= -(1 << 20) || v >= (1 << 20)) continue;
+                bad += mul_whole20(bits(w), v) != bits(want);
                 ++checked;
             }
         // every |v| < 2^20 against a few weights
@@ -104,7 +104,7 @@ int main()
                 bad += mul_whole20(bits(w), v) != bits(w * static_cast<double>(v));
                 ++checked;
             }
-        std::printf("mul_whole checked=%ld\n", checked);
+        std::printf("mul_whole20 checked=%ld\n", checked);
     }
     std::printf("bad=%d\n", bad);
     return bad != 0;
