@@ -125,4 +125,16 @@ __device__ __forceinline__ void df_add(float& o_hi, float& o_lo, float s_hi, flo
     fast_two_sum(t, e, o_hi, o_lo);
 }
 
+// (o_hi, o_lo) += (s_hi, s_lo) without renormalising: o_hi takes the rounded sum of the high parts
+// and o_lo collects its exact error and the low parts. A series of these (out held in registers
+// across applications) ends with one fast_two_sum(o_hi, o_lo); o_lo stays a small multiple of the
+// rounding errors, far inside FP32's range, so the pair keeps its accuracy.
+__device__ __forceinline__ void df_add_lazy(float& o_hi, float& o_lo, float s_hi, float s_lo)
+{
+    float t, e;
+    two_sum(o_hi, s_hi, t, e);
+    o_hi = t;
+    o_lo = __fadd_rn(o_lo, __fadd_rn(e, s_lo));
+}
+
 }  // namespace prk

@@ -193,10 +193,13 @@ __device__ __forceinline__ void fp32c_points(const float* s, int ld, float (&sh)
     constexpr int SEG = CPT + 2 * RA;
     constexpr int NG = group_count<P, R>();
     float D[NG][CPT];
+    bool seen[NG];  // a group's sum starts from its first difference (known once the loops unroll)
 #pragma unroll
-    for (int g = 0; g < NG; ++g)
+    for (int g = 0; g < NG; ++g) {
+        seen[g] = false;
 #pragma unroll
         for (int k = 0; k < CPT; ++k) D[g][k] = 0.0f;
+    }
     {
         float m0[SEG];
         ld_seg<SEG>(s - RA, m0);
@@ -205,7 +208,11 @@ __device__ __forceinline__ void fp32c_points(const float* s, int ld, float (&sh)
             constexpr int dr = 0;
             const int g = group_of<P, R>(dc, dr);
 #pragma unroll
-            for (int k = 0; k < CPT; ++k) D[g][k] = __fadd_rn(D[g][k], __fsub_rn(m0[k + RA + dc], m0[k + RA - dc]));
+            for (int k = 0; k < CPT; ++k) {
+                const float d = __fsub_rn(m0[k + RA + dc], m0[k + RA - dc]);
+                D[g][k] = seen[g] ? __fadd_rn(D[g][k], d) : d;
+            }
+            seen[g] = true;
         }
     }
 #pragma unroll
@@ -216,7 +223,11 @@ __device__ __forceinline__ void fp32c_points(const float* s, int ld, float (&sh)
             ld_seg<CPT>(s - dr * ld, dn);
             const int g = group_of<P, R>(0, dr);
 #pragma unroll
-            for (int k = 0; k < CPT; ++k) D[g][k] = __fadd_rn(D[g][k], __fsub_rn(up[k], dn[k]));
+            for (int k = 0; k < CPT; ++k) {
+                const float d = __fsub_rn(up[k], dn[k]);
+                D[g][k] = seen[g] ? __fadd_rn(D[g][k], d) : d;
+            }
+            seen[g] = true;
         } else {
             float up[SEG], dn[SEG];
             ld_seg<SEG>(s + dr * ld - RA, up);
@@ -229,8 +240,12 @@ __device__ __forceinline__ void fp32c_points(const float* s, int ld, float (&sh)
 #pragma unroll
                     for (int k = 0; k < CPT; ++k) {
                         const float d = __fsub_rn(up[k + RA + dc], dn[k + RA - dc]);
-                        D[g][k] = sg > 0 ? __fadd_rn(D[g][k], d) : __fsub_rn(D[g][k], d);
+                        if (seen[g])
+                            D[g][k] = sg > 0 ? __fadd_rn(D[g][k], d) : __fsub_rn(D[g][k], d);
+                        else
+                            D[g][k] = sg > 0 ? d : -d;
                     }
+                    seen[g] = true;
                 }
             }
         }
@@ -889,7 +904,10 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
             for (int k = 0; k < CPT; ++k) {
                 float oh = __uint_as_float(static_cast<uint32_t>(o[k]));
                 float ol = __uint_as_float(static_cast<uint32_t>(o[k] >> 32));
-                df_add(oh, ol, sh[k], sl[k]);
+                if constexpr (STEPS == 1)
+                    df_add(oh, ol, sh[k], sl[k]);
+                else  // out stays in registers: renormalised once, before it is stored
+                    df_add_lazy(oh, ol, sh[k], sl[k]);
                 o[k] = static_cast<uint64_t>(__float_as_uint(oh)) | (static_cast<uint64_t>(__float_as_uint(ol)) << 32);
             }
         }
@@ -1094,6 +1112,18 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
             for (int rr = 0; rr < ROWS; ++rr)
                 if (ract[rr]) apply_row(warp * ROWS + rr, o[rr]);
         }
+        }
+        if constexpr (DT == FP32C) {  // the pairs accumulated without renormalising
+#pragma unroll
+            for (int rr = 0; rr < ROWS; ++rr)
+#pragma unroll
+                for (int k = 0; k < CPT; ++k) {
+                    float oh, ol;
+                    fast_two_sum(__uint_as_float(static_cast<uint32_t>(o[rr][k])),
+                                 __uint_as_float(static_cast<uint32_t>(o[rr][k] >> 32)), oh, ol);
+                    o[rr][k] = static_cast<uint64_t>(__float_as_uint(oh)) |
+                               (static_cast<uint64_t>(__float_as_uint(ol)) << 32);
+                }
         }
         if (oint) {
 #pragma unroll
