@@ -109,6 +109,32 @@ PRK_HD int clz32(uint32_t x)
 #endif
 }
 
+// mul_whole20 (below) with the weight pre-split, as a table entry holds it: w1 = the low 32 bits of
+// w's significand W, w2 = its high 21 bits with the hidden bit, hib = w's sign and biased exponent
+// field as in the encoding's high word.
+PRK_HD uint64_t mul_whole20_split(uint32_t w1, uint32_t w2, uint32_t hib, int32_t v)
+{
+    const uint32_t vs = static_cast<uint32_t>(v) & 0x80000000u;
+    const uint32_t a = static_cast<uint32_t>(v < 0 ? -v : v);
+    const uint64_t x = static_cast<uint64_t>(w1) * a;
+    const uint64_t y = static_cast<uint64_t>(w2) * a;
+    const uint64_t mid = (x >> 32) + (y & 0xFFFFFFFFull);
+    const uint32_t p0 = static_cast<uint32_t>(x), p1 = static_cast<uint32_t>(mid);
+    const uint32_t p2 = static_cast<uint32_t>((y >> 32) + (mid >> 32));
+    const int sh = (p2 ? 96 - clz32(p2) : 64 - clz32(p1)) - 53;
+    const uint32_t q_lo = static_cast<uint32_t>(((static_cast<uint64_t>(p1) << 32) | p0) >> (sh & 63));
+    const uint32_t q_hi = static_cast<uint32_t>(((static_cast<uint64_t>(p2) << 32) | p1) >> (sh & 63));
+    const uint32_t mask = (1u << (sh & 31)) - 1u, rem = p0 & mask;
+    // round to nearest-even: add half - 1 + (lowest kept bit) to the bits below, carry into q
+    const uint32_t bump = (rem + (mask >> 1) + (sh > 0 ? (q_lo & 1u) : 0u)) >> (sh & 31);
+    const uint64_t q = ((static_cast<uint64_t>(q_hi) << 32) | q_lo) + (sh > 0 ? bump : 0u);
+    const uint32_t ovf = static_cast<uint32_t>(q >> 53);  // 1 when rounding carried to 2^53
+    const uint32_t hi = ((hib ^ vs) & 0x80000000u) | ((hib & 0x7FF00000u) + ((static_cast<uint32_t>(sh) + ovf) << 20)) |
+                        (static_cast<uint32_t>(q >> (32 + ovf)) & 0xFFFFFu);
+    const uint32_t lo = static_cast<uint32_t>(q >> ovf);
+    return v == 0 ? static_cast<uint64_t>(hib & 0x80000000u) << 32 : (static_cast<uint64_t>(hi) << 32) | lo;
+}
+
 // Bits of fl(w * v), the binary64 product rounded to nearest-even, for a normal binary64 w (encoding
 // wb, biased exponent at most 2025) and a whole number |v| < 2^20, from integer operations on w's
 // 53-bit significand W: W * |v| < 2^73 is formed as three 32-bit words from two 32 x 32 -> 64-bit
@@ -117,26 +143,7 @@ PRK_HD int clz32(uint32_t x)
 PRK_HD uint64_t mul_whole20(uint64_t wb, int32_t v)
 {
     const uint32_t whi = static_cast<uint32_t>(wb >> 32);
-    if (v == 0) return static_cast<uint64_t>(whi & 0x80000000u) << 32;
-    const uint32_t sign = (whi ^ (v < 0 ? 0x80000000u : 0u)) & 0x80000000u;
-    const uint32_t a = static_cast<uint32_t>(v < 0 ? -v : v);
-    const uint64_t x = static_cast<uint64_t>(static_cast<uint32_t>(wb)) * a;  // low word of W times a, < 2^52
-    const uint64_t y = static_cast<uint64_t>((whi & 0xFFFFFu) | 0x100000u) * a;  // high 21 bits, < 2^41
-    const uint64_t mid = (x >> 32) + (y & 0xFFFFFFFFull);
-    const uint32_t p0 = static_cast<uint32_t>(x), p1 = static_cast<uint32_t>(mid);
-    const uint32_t p2 = static_cast<uint32_t>((y >> 32) + (mid >> 32));  // W * a = p2:p1:p0, p2 < 2^9
-    const int sh = (p2 ? 96 - clz32(p2) : 64 - clz32(p1)) - 53;          // bits rounded away, 0..20
-    const uint32_t q_lo = static_cast<uint32_t>(((static_cast<uint64_t>(p1) << 32) | p0) >> sh);
-    const uint32_t q_hi = static_cast<uint32_t>(((static_cast<uint64_t>(p2) << 32) | p1) >> sh);
-    const uint32_t mask = (1u << sh) - 1u, rem = p0 & mask, half = (mask >> 1) + (sh > 0 ? 1u : 0u);
-    const bool up = sh > 0 && (rem > half || (rem == half && (q_lo & 1u)));
-    uint64_t q = ((static_cast<uint64_t>(q_hi) << 32) | q_lo) + (up ? 1u : 0u);
-    uint32_t e = ((whi >> 20) & 0x7FFu) + static_cast<uint32_t>(sh);
-    if (q >> 53) {
-        q >>= 1;
-        ++e;
-    }
-    return (static_cast<uint64_t>(sign | (e << 20)) << 32) | (q & MANT);
+    return mul_whole20_split(static_cast<uint32_t>(wb), (whi & 0xFFFFFu) | 0x100000u, whi & 0xFFF00000u, v);
 }
 
 // Certification of a tile whose values have lowest-bit exponents >= lo_min and highest-bit

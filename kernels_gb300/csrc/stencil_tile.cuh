@@ -614,13 +614,14 @@ static_assert(encode(1.0) == 0x3FF0000000000000ull && encode(-0.125) == 0xBFC000
               "constexpr binary64 encoding");
 
 // The taps of a stencil in the generator's order (column offset outer, row offset inner, zero
-// weights left out), with their offsets in a tile of row length LD and their weights' encodings.
+// weights left out), with their offsets in a tile of row length LD and their weights split for
+// fx::mul_whole20_split: the significand's low 32 bits, its high 21 bits with the hidden bit, and
+// the sign and exponent field of the encoding's high word. One 16-byte entry per tap.
 template <int P, int R, int LD>
 struct TapTable {
-    struct Tap {
+    struct alignas(16) Tap {
         int off;
-        int pad;
-        uint64_t wb;
+        uint32_t w1, w2, hib;
     } tap[tap_count(P, R)];
 };
 
@@ -633,9 +634,11 @@ constexpr TapTable<P, R, LD> make_taps()
         for (int dr = -R; dr <= R; ++dr) {
             const double w = weight(P, R, dc, dr);
             if (w != 0.0) {
+                const uint64_t wb = encode(w);
                 t.tap[k].off = dr * LD + dc;
-                t.tap[k].pad = 0;
-                t.tap[k].wb = encode(w);
+                t.tap[k].w1 = static_cast<uint32_t>(wb);
+                t.tap[k].w2 = static_cast<uint32_t>((wb >> 32) & 0xFFFFFu) | 0x100000u;
+                t.tap[k].hib = static_cast<uint32_t>(wb >> 32) & 0xFFF00000u;
                 ++k;
             }
         }
@@ -646,7 +649,7 @@ template <int P, int R, int LD>
 __constant__ TapTable<P, R, LD> c_taps = make_taps<P, R, LD>();
 
 // fp64_point for CPT adjacent points of a tile of whole numbers |v| < 2^20 held as int32: every
-// product comes from fx::mul_whole20 on the integer pipes (the same bits as __dmul_rn), every sum is
+// product comes from fx::mul_whole20_split on the integer pipes (the same bits as __dmul_rn), every sum is
 // the same binary64 add in the same order, so the binary64 pipe issues one instruction per tap
 // instead of two. The taps come from constant memory in a loop, which keeps the code small.
 template <int P, int R, int LD, int CPT>
@@ -654,16 +657,20 @@ __device__ __forceinline__ void fp64_points_whole(const int32_t* s, double (&acc
 {
     constexpr int N = tap_count(P, R);
     const auto& T = c_taps<P, R, LD>;
-#pragma unroll
-    for (int k = 0; k < CPT; ++k)
-        acc[k] = __longlong_as_double(static_cast<long long>(fx::mul_whole20(T.tap[0].wb, s[T.tap[0].off + k])));
-#pragma unroll 2
-    for (int t = 1; t < N; ++t) {
-        const int off = T.tap[t].off;
-        const uint64_t wb = T.tap[t].wb;
+    {
+        const auto tp = T.tap[0];
 #pragma unroll
         for (int k = 0; k < CPT; ++k)
-            acc[k] = __dadd_rn(acc[k], __longlong_as_double(static_cast<long long>(fx::mul_whole20(wb, s[off + k]))));
+            acc[k] = __longlong_as_double(
+                static_cast<long long>(fx::mul_whole20_split(tp.w1, tp.w2, tp.hib, s[tp.off + k])));
+    }
+#pragma unroll 2
+    for (int t = 1; t < N; ++t) {
+        const auto tp = T.tap[t];
+#pragma unroll
+        for (int k = 0; k < CPT; ++k)
+            acc[k] = __dadd_rn(acc[k], __longlong_as_double(static_cast<long long>(
+                                           fx::mul_whole20_split(tp.w1, tp.w2, tp.hib, s[tp.off + k]))));
     }
 }
 

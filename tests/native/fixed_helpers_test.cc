@@ -96,12 +96,20 @@ int main()
                 const double want = w * static_cast<double>(v);
                 if (v <= -(1 << 20) || v >= (1 << 20)) continue;
                 bad += mul_whole20(bits(w), v) != bits(want);
+                {
+                    const uint64_t wb = bits(w);
+                    const uint32_t w1 = static_cast<uint32_t>(wb), w2 = static_cast<uint32_t>((wb >> 32) & 0xFFFFFu) | 0x100000u;
+                    bad += mul_whole20_split(w1, w2, static_cast<uint32_t>(wb >> 32) & 0xFFF00000u, v) != bits(want);
+                }
                 ++checked;
             }
         // every |v| < 2^20 against a few weights
         for (double w : {1.0 / 6.0, -1.0 / 18.0, 1.0 / 48.0, -1.0 / 100.0, 1.0 / 30.0})
             for (int32_t v = -(1 << 20) + 1; v < (1 << 20); ++v) {
                 bad += mul_whole20(bits(w), v) != bits(w * static_cast<double>(v));
+                const uint64_t wb = bits(w);
+                const uint32_t w1 = static_cast<uint32_t>(wb), w2 = static_cast<uint32_t>((wb >> 32) & 0xFFFFFu) | 0x100000u;
+                bad += mul_whole20_split(w1, w2, static_cast<uint32_t>(wb >> 32) & 0xFFF00000u, v) != bits(w * static_cast<double>(v));
                 ++checked;
             }
         std::printf("mul_whole20 checked=%ld\n", checked);
