@@ -133,3 +133,36 @@ def test_whole_run_rejections(cuda):
     in_a, in_b, out = kg.alloc(64, kg.FP64)
     with pytest.raises(kg.PrkError):
         kg.run(kg.STAR, 2, 3, in_a, None, out, whole=True, unfused=True)
+
+
+@pytest.mark.parametrize("n", [8, 64, 130])
+@pytest.mark.parametrize("dtype", [kg.FP64, kg.FP32C])
+def test_run_host_smallest_shapes(cuda, n, dtype):
+    """One band (n below the band height), the smallest TMA shapes, and a ragged FP32C size."""
+    if dtype == kg.FP32C and n % 4:
+        n += 4 - n % 4
+    r, k = 1, 3
+    _, ref = po.run(kg.STAR, r, n, k)
+    if dtype == kg.FP64:
+        h_in = np.add.outer(np.arange(n), np.arange(n)).astype(np.float64)
+        h_out = np.zeros((n, n))
+    else:
+        h_in = np.add.outer(np.arange(n), np.arange(n)).astype(np.float32)
+        h_out = np.zeros((n, n, 2), np.float32)
+    res = kg.run_host(kg.STAR, r, k, h_in, h_out)
+    got = h_out if dtype == kg.FP64 else h_out.astype(np.float64).sum(axis=-1)
+    inner = (slice(r, n - r), slice(r, n - r))
+    if dtype == kg.FP64:
+        assert np.array_equal(bits(got), bits(ref))
+    else:
+        assert (np.abs(got[inner] - ref[inner]) / np.abs(ref[inner])).max() <= 1e-6
+    assert abs(res["norm"] - 2.0 * (k + 1)) <= 1e-8
+
+
+def test_whole_run_of_one_timed_application(cuda):
+    n, k = 96, 1
+    _, ref = po.run(kg.GRID, 2, n, k)
+    in_a, in_b, out = kg.alloc(n, kg.FP64)
+    kg.init(in_a, out)
+    kg.run(kg.GRID, 2, k, in_a, in_b, out, whole=True)
+    assert np.array_equal(bits(out.cpu().numpy()), bits(ref))
