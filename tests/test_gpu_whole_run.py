@@ -166,3 +166,40 @@ def test_whole_run_of_one_timed_application(cuda):
     kg.init(in_a, out)
     kg.run(kg.GRID, 2, k, in_a, in_b, out, whole=True)
     assert np.array_equal(bits(out.cpu().numpy()), bits(ref))
+
+
+@pytest.mark.parametrize("pattern,r", [(kg.STAR, 2), (kg.GRID, 3)])
+def test_whole_run_full_size_sampled(cuda, pattern, r):
+    """n=16384, 100 timed iterations in one launch per tile (the FP32 route for star R=2, integer
+    products for grid R=3): the norm, sampled points against the per-point oracle bit for bit,
+    tile corners included, and the final `in`."""
+    n, K = 16384, 100
+    in_a, in_b, out = kg.alloc(n, kg.FP64)
+    kg.init(in_a, out)
+    res = kg.run(pattern, r, K, in_a, in_b, out, whole=True)
+    assert abs(kg.norm(r, out) - 2.0 * (K + 1)) <= 1e-8
+    rng = np.random.default_rng(17 + r)
+    pts = [(r, r), (n - r - 1, n - r - 1), (r, n - r - 1), (31, 63), (32, 64), (8191, 8192)] + \
+          [tuple(int(x) for x in rng.integers(r, n - r, 2)) for _ in range(60)]
+    idx = cuda.tensor([i * n + j for i, j in pts], device="cuda")
+    got = out.reshape(-1)[idx].cpu().numpy()
+    for (i, j), v in zip(pts, got):
+        assert v == po.point(pattern, r, n, K + 1, i, j), (i, j)
+    fin = res.final_in.reshape(-1)[idx].cpu().numpy()
+    assert all(f == i + j + K + 1 for (i, j), f in zip(pts, fin))
+
+
+def test_run_host_banded_full_size_sampled(cuda):
+    """The banded host-buffer run at n=16384 with pinned buffers, sampled against the oracle."""
+    n, K, r = 16384, 20, 2
+    idx = cuda.arange(n, dtype=cuda.float64)
+    h_in = (idx[:, None] + idx[None, :]).pin_memory()
+    h_out = cuda.zeros((n, n), dtype=cuda.float64).pin_memory()
+    res = kg.run_host(kg.STAR, r, K, h_in, h_out)
+    assert abs(res["norm"] - 2.0 * (K + 1)) <= 1e-8
+    rng = np.random.default_rng(5)
+    pts = [(r, r), (n - r - 1, n - r - 1), (511, 1000), (512, 1000), (513, 7)] + \
+          [tuple(int(x) for x in rng.integers(r, n - r, 2)) for _ in range(40)]
+    out = h_out.numpy()
+    for i, j in pts:
+        assert out[i, j] == po.point(kg.STAR, r, n, K + 1, i, j), (i, j)
