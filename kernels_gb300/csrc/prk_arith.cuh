@@ -11,6 +11,7 @@
 //  df_add             (hi, lo) += (s_hi, s_lo) for the two-float out accumulator.
 #pragma once
 
+#include "prk_fixed.cuh"
 #include "prk_stencil.cuh"
 
 namespace prk {
@@ -101,18 +102,13 @@ __device__ __forceinline__ void fp32c_point(const float* s, int ld, float& s_hi,
     s_lo = lo;
 }
 
-// fl(a + 1) without the binary64 pipe where that is exact: for a positive whole number
-// 1 <= a < 2^53 the sum's encoding is a's plus one unit of the integer position (the mantissa's
-// 2^(1075 - e) bit; its carry steps the exponent when the mantissa overflows). Other values take
-// the binary64 add.
+// fl(a + 1) without the binary64 pipe where that is exact (fx::inc_whole: positive whole numbers
+// below 2^53); other values take the binary64 add.
 __device__ __forceinline__ double inc_exact(double a)
 {
-    const uint64_t b = static_cast<uint64_t>(__double_as_longlong(a));
-    const int e = static_cast<int>(b >> 52);  // >= 2048 for negative a
-    if (e >= 1023 && e <= 1075) {
-        const uint64_t unit = 1ull << (1075 - e);
-        if ((b & (unit - 1)) == 0) return __longlong_as_double(static_cast<long long>(b + unit));
-    }
+    uint64_t r;
+    if (fx::inc_whole(static_cast<uint64_t>(__double_as_longlong(a)), &r))
+        return __longlong_as_double(static_cast<long long>(r));
     return __dadd_rn(a, 1.0);
 }
 

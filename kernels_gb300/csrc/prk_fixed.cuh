@@ -100,6 +100,20 @@ PRK_HD uint64_t from_fixed(int64_t x, int unit)
     return s | ((static_cast<uint64_t>(msb + unit + 1022) << 52) + m);
 }
 
+// The encoding of a + 1 for a positive whole number 1 <= a < 2^53 (encoding b): a's encoding plus
+// one unit of the integer position, the mantissa's 2^(1075 - e) bit, whose carry steps the
+// exponent when the mantissa overflows (a = 2^k - 1). Returns false, leaving *r alone, for any other
+// value (negative, fractional, zero, subnormal, at or above 2^53, infinite or NaN).
+PRK_HD bool inc_whole(uint64_t b, uint64_t* r)
+{
+    const int e = static_cast<int>(b >> 52);  // >= 2048 for negative values
+    if (e < 1023 || e > 1075) return false;
+    const uint64_t unit = 1ull << (1075 - e);
+    if (b & (unit - 1)) return false;
+    *r = b + unit;
+    return true;
+}
+
 PRK_HD int clz32(uint32_t x)
 {
 #ifdef __CUDA_ARCH__

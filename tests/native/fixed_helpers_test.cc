@@ -114,6 +114,29 @@ int main()
             }
         std::printf("mul_whole20 checked=%ld\n", checked);
     }
+    // inc_whole against the host's a + 1.0: random whole numbers below 2^53, 2^k - 1 (the carry into
+    // the exponent), powers of two, and values it must refuse (then a + 1.0 is left to binary64)
+    {
+        std::vector<double> as = {0.0, -0.0, -1.0, -5.0, 0.5, 1.5, 0x1p53, 0x1p52 + 2.0, INFINITY, NAN, 5e-324, 1.0};
+        for (int k = 1; k < 54; ++k) {
+            as.push_back(std::ldexp(1.0, k) - 1.0);
+            as.push_back(std::ldexp(1.0, k));
+        }
+        for (int t = 0; t < 200000; ++t) as.push_back(static_cast<double>(g() >> 11));
+        for (int t = 0; t < 1000; ++t) as.push_back(std::ldexp(static_cast<double>(g() >> 11), -20) * (g() & 1 ? 1 : -1));
+        long checked = 0, certified = 0;
+        for (double a : as) {
+            uint64_t r;
+            if (inc_whole(bits(a), &r)) {
+                bad += r != bits(a + 1.0);
+                ++certified;
+            } else {
+                bad += (a >= 1.0 && a < 0x1p53 && a == std::floor(a));  // a whole number it should take
+            }
+            ++checked;
+        }
+        std::printf("inc_whole checked=%ld certified=%ld\n", checked, certified);
+    }
     std::printf("bad=%d\n", bad);
     return bad != 0;
 }
