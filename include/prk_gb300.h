@@ -158,7 +158,8 @@ int prk_gb300_status(void);
 typedef struct {
     int depth;                      /* applications per launch: 1, 2, 4 or 8; 0: every timed
                                        application in one launch (PRK_RUN_WHOLE) */
-    int kernel;                     /* 1 = generic kernels, 2 = TMA tile kernels, 3 = batched kernel */
+    int kernel;                     /* 1 = generic kernels, 2 = TMA tile kernels, 3 = batched kernel,
+                                       4 = plain-staged tile kernels (shapes TMA cannot take) */
     int tile_rows;                  /* tile shape (rows x columns) of the chosen kernel */
     int tile_cols;
     int cols_per_thread;            /* thread coarsening: adjacent columns each thread owns */

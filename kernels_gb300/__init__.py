@@ -219,7 +219,7 @@ def tune(pattern: int, radius: int, n: int, dtype: int = FP64, batch: bool = Fal
     from ._lib import Tuning
     t = Tuning()
     check(load().prk_gb300_tune(pattern, radius, n, dtype, (1 if batch else 0) | (2 if force else 0), C.byref(t)))
-    return {"depth": t.depth, "kernel": {1: "generic", 2: "tma", 3: "batched"}.get(t.kernel, str(t.kernel)),
+    return {"depth": t.depth, "kernel": {1: "generic", 2: "tma", 3: "batched", 4: "plain"}.get(t.kernel, str(t.kernel)),
             "tile_rows": t.tile_rows, "tile_cols": t.tile_cols, "cols_per_thread": t.cols_per_thread,
             "seconds_per_application": t.seconds_per_application, "from_cache": bool(t.from_cache)}
 

@@ -124,12 +124,15 @@ thread_local int t_tile_rows = 32;
 int launch_one(int pattern, int radius, int64_t n, int dtype, const void* in, void* in_next, void* out, cudaStream_t s)
 {
     prk::StencilCall c{pattern, radius, n, dtype, in, in_next, out, s};
-    const bool tma = g_kernel_choice != 1 && !t_force_generic && prk::tma_eligible(c);
+    const bool tiles = g_kernel_choice != 1 && !t_force_generic;
+    const bool tma = tiles && prk::tma_eligible(c);
     if (g_kernel_choice == 2 && !tma) return fail(PRK_ERR_ARG, "the TMA tile kernel was required but the call is not eligible");
     if (tma) {
         DevScratch d;
         if (int rc = dev_scratch(&d)) return rc;
         PRK_CUDA(prk::launch_stencil_tma(c, 1, d.status, t_tile_rows), "stencil launch (TMA tiles)");
+    } else if (tiles && prk::plain_eligible(c)) {
+        PRK_CUDA(prk::launch_stencil_plain(c, 1), "stencil launch (plain-staged tiles)");
     } else {
         PRK_CUDA(prk::launch_stencil_generic(c), "stencil launch");
     }
@@ -142,9 +145,14 @@ int launch_steps(int pattern, int radius, int64_t n, int dtype, int steps, const
 {
     prk::StencilCall c{pattern, radius, n, dtype, in, in_next, out, s};
     if (!prk::tma_depth_ok(steps)) return fail(PRK_ERR_ARG, "temporal depth %d is not 1, 2, 4 or 8", steps);
-    if (!prk::tma_eligible(c) || g_kernel_choice == 1)
-        return fail(PRK_ERR_ARG, "temporal blocking needs the TMA tile kernels: 16-byte-aligned buffers, n a multiple of %d",
-                    dtype == PRK_FP64 ? 2 : 4);
+    if (g_kernel_choice == 1) return fail(PRK_ERR_ARG, "temporal blocking needs the tile kernels");
+    if (!prk::tma_eligible(c)) {
+        if (g_kernel_choice == 2 || !prk::plain_eligible(c))
+            return fail(PRK_ERR_ARG, "temporal blocking needs the tile kernels: buffers aligned to their element size%s",
+                        g_kernel_choice == 2 ? ", 16-byte-aligned with n a multiple of the vector width for TMA" : "");
+        PRK_CUDA(prk::launch_stencil_plain(c, steps), "stencil launch (plain-staged tiles, temporal)");
+        return PRK_OK;
+    }
     DevScratch d;
     if (int rc = dev_scratch(&d)) return rc;
     PRK_CUDA(prk::launch_stencil_tma(c, steps, d.status, t_tile_rows), "stencil launch (TMA tiles, temporal)");
@@ -313,7 +321,9 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
     int cur = 0;
     {
         prk::StencilCall probe{pattern, radius, n, dtype, in_a, in_b, out, nullptr};
-        if (unfused || g_kernel_choice == 1 || t_force_generic || !prk::tma_eligible(probe)) depth = 1;
+        if (unfused || g_kernel_choice == 1 || t_force_generic ||
+            (!prk::tma_eligible(probe) && (g_kernel_choice == 2 || !prk::plain_eligible(probe))))
+            depth = 1;
     }
     auto step = [&](cudaStream_t st) -> int {
         if (unfused) {
@@ -325,20 +335,25 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
         }
         return PRK_OK;
     };
+    bool whole_tma = true;
     if (whole) {
         prk::StencilCall probe{pattern, radius, n, dtype, in_a, in_b, out, nullptr};
-        if (g_kernel_choice == 1 || !prk::tma_eligible(probe))
-            return fail(PRK_ERR_ARG, "PRK_RUN_WHOLE needs the TMA tile kernels: 16-byte-aligned buffers, n a multiple of %d",
-                        dtype == PRK_FP64 ? 2 : 4);
+        whole_tma = prk::tma_eligible(probe);
+        if (g_kernel_choice == 1 || (!whole_tma && (g_kernel_choice == 2 || !prk::plain_eligible(probe))))
+            return fail(PRK_ERR_ARG, "PRK_RUN_WHOLE needs the tile kernels: buffers aligned to their element size");
     }
     // `count` applications: one launch (whole run), or launches of the temporal depth with the
     // remainder in powers of two.
     auto steps = [&](cudaStream_t st, int count) -> int {
         if (whole) {
-            DevScratch dsc;
-            if (int rc = dev_scratch(&dsc)) return rc;
             prk::StencilCall c{pattern, radius, n, dtype, bufs[cur], bufs[cur ^ 1], out, st};
-            PRK_CUDA(prk::launch_stencil_tma_band(c, count, 0, n, dsc.status), "stencil launch (TMA tiles, whole run)");
+            if (whole_tma) {
+                DevScratch dsc;
+                if (int rc = dev_scratch(&dsc)) return rc;
+                PRK_CUDA(prk::launch_stencil_tma_band(c, count, 0, n, dsc.status), "stencil launch (TMA tiles, whole run)");
+            } else {
+                PRK_CUDA(prk::launch_stencil_plain(c, count), "stencil launch (plain-staged tiles, whole run)");
+            }
             cur ^= 1;
             return PRK_OK;
         }

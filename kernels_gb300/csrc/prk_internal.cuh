@@ -42,6 +42,12 @@ cudaError_t launch_stencil_tma(const StencilCall& c, int steps, unsigned* status
 // rows, writes the band's in_next (in after `depth` updates) and out rows.
 cudaError_t launch_stencil_tma_band(const StencilCall& c, int depth, int64_t row0, int64_t rows, unsigned* status);
 
+// tile_plain_*.cu: the fused form on shapes the TMA kernels cannot take (any n, buffers aligned to
+// their element size); the tile staged with plain loads, then evaluated as in the TMA kernels.
+// `depth` applications in one launch (1 for one application per launch).
+bool plain_eligible(const StencilCall& c);
+cudaError_t launch_stencil_plain(const StencilCall& c, int depth);
+
 // kernels_generic.cu: any n, any 8-byte-aligned pointers.
 cudaError_t launch_stencil_generic(const StencilCall& c);
 cudaError_t launch_add(int64_t n, int dtype, void* in, cudaStream_t s);

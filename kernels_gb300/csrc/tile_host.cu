@@ -1,11 +1,12 @@
-// Host side of the TMA tile kernels: eligibility, tensor-map encoding and dispatch to the
-// per-form instantiations (tile_*.cu). cuTensorMapEncodeTiled is fetched from the driver at run
-// time, so the library does not link libcuda.
+// Host side of the tile kernels: eligibility, tensor-map encoding and dispatch to the per-form
+// instantiations of the TMA kernel (tile_*.cu) and of the plain-staging kernel (tile_plain_*.cu).
+// cuTensorMapEncodeTiled is fetched from the driver at run time, so the library does not link
+// libcuda.
 #include <cudaTypedefs.h>
 
 #include <mutex>
 
-#include "stencil_tile.cuh"
+#include "tile_plain.cuh"
 
 namespace prk {
 namespace {
@@ -92,6 +93,36 @@ cudaError_t launch_stencil_tma(const StencilCall& c, int steps, unsigned* status
 {
     if (!tma_depth_ok(steps) || !tma_rows_ok(tile_rows)) return cudaErrorInvalidValue;
     return launch_tma(c, steps, status, tile_rows, 0, 0, 0);
+}
+
+bool plain_eligible(const StencilCall& c)
+{
+    if (!c.in_next || c.n > NMAX) return false;
+    auto al = [](const void* p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; };
+    const uintptr_t e = c.dtype == FP64 ? 8 : 4;
+    return al(c.in, e) && al(c.in_next, e) && al(c.out, 8);
+}
+
+cudaError_t launch_stencil_plain(const StencilCall& c, int depth)
+{
+    if (depth < 1 || !plain_eligible(c)) return cudaErrorInvalidValue;
+    using CF = tile::Cfg<FP64>;
+    using CC = tile::Cfg<FP32C>;
+    batch::GridDesc g{};
+    g.n = c.n;
+    g.in[0] = const_cast<void*>(c.in);
+    g.in[1] = c.in_next;
+    g.out = c.out;
+    g.pattern = c.pattern;
+    g.R = c.R;
+    const int tw = c.dtype == FP64 ? CF::TW : CC::TW;
+    const int th = c.dtype == FP64 ? CF::TH : CC::TH;
+    g.tiles_x = static_cast<int>((c.n + tw - 1) / tw);
+    g.tiles = ((c.n + th - 1) / th) * g.tiles_x;
+    g.vec_ok = 0;
+    const int steps = depth == 1 ? 1 : 0;
+    return c.dtype == FP64 ? plain::launch_fp64(c.pattern, c.R, steps, g, depth, c.stream)
+                           : plain::launch_fp32c(c.pattern, c.R, steps, g, depth, c.stream);
 }
 
 cudaError_t launch_stencil_tma_band(const StencilCall& c, int depth, int64_t row0, int64_t rows, unsigned* status)

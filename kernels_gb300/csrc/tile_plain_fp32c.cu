@@ -1,0 +1,14 @@
+// Instantiations of the plain-staging tile kernel for FP32C storage (FP32 with compensated
+// accumulation): star and grid, R=1..5, one application per launch and run-time depth.
+#include "tile_plain.cuh"
+
+namespace prk {
+namespace plain {
+
+cudaError_t launch_fp32c(int pattern, int R, int steps, const batch::GridDesc& g, int depth, cudaStream_t s)
+{
+    return launch_form<FP32C>(pattern, R, steps, g, depth, s);
+}
+
+}  // namespace plain
+}  // namespace prk

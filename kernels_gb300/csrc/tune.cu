@@ -1,9 +1,10 @@
 // The autotuner (prk_gb300_tune): times the candidate kernel configurations for a (pattern, radius,
 // n, dtype) on scratch buffers and keeps the fastest in memory and in a JSON-lines cache file.
 //
-// Candidates, single grid: the TMA tile kernels with tiles of 32 and of 64 rows (4 or 8 rows per
-// thread) at temporal depth 1, 2, 4 and 8 and with the whole run in one launch (when the shape
-// allows TMA: n a multiple of the vector width), and the generic kernels. Batched grids: the
+// Candidates, single grid: the tile kernels at temporal depth 1, 2, 4 and 8 and with the whole run
+// in one launch, and the generic kernels. The tile kernels are the TMA ones, with tiles of 32 and of
+// 64 rows (4 or 8 rows per thread), when the shape allows TMA (n a multiple of the vector width),
+// else the plain-staged ones with tiles of 32 rows. Batched grids: the
 // batched kernel at depth 1, 2, 4 and 8 and with the whole run in one launch. Every candidate
 // computes the same bits (FP64) or stays within the FP32C bound, so the choice affects speed only.
 #include <cstdio>
@@ -139,7 +140,7 @@ extern "C" int prk_gb300_tune(int pattern, int radius, int64_t n, int dtype, int
     char keybuf[512];
     std::snprintf(keybuf, sizeof keybuf, "%s|sm%d%d|%s|R%d|%s|n%lld|%s%s|v2", prop.name, prop.major, prop.minor,
                   pattern == PRK_STAR ? "star" : "grid", radius, dtype == PRK_FP64 ? "fp64" : "fp32c",
-                  static_cast<long long>(bucket(n)), batch ? "batch" : "single", tma_shape ? "" : "|generic");
+                  static_cast<long long>(bucket(n)), batch ? "batch" : "single", tma_shape ? "" : "|plain");
     const std::string key = keybuf;
     std::lock_guard<std::mutex> lock(g_mu);
     load_cache();
@@ -176,27 +177,26 @@ extern "C" int prk_gb300_tune(int pattern, int radius, int64_t n, int dtype, int
             if (batch) {
                 rc = time_batch(pattern, radius, m, dtype, d, s, &sec);
             } else {
-                if (!tma_shape && d > 1) continue;
                 rc = time_run(pattern, radius, m, dtype, PRK_RUN_DEPTH(d) | (tall ? PRK_RUN_TALL : 0), s, &sec);
             }
             if (rc) break;
             if (sec < best.seconds_per_application) {
-                best = prk_gb300_tuning{d, (batch || !tma_shape) ? 1 : 2, tall ? 64 : th, tw, cpt, sec, 0};
+                best = prk_gb300_tuning{d, tma_shape ? 2 : 4, tall ? 64 : th, tw, cpt, sec, 0};
                 if (batch) best.kernel = 3;
             }
         }
     }
-    if (!rc && !batch && tma_shape) {  // the whole run in one launch
+    if (!rc && !batch) {  // the whole run in one launch
         double sec = 0.0;
         rc = time_run(pattern, radius, m, dtype, PRK_RUN_WHOLE, s, &sec);
-        if (!rc && sec < best.seconds_per_application) best = prk_gb300_tuning{0, 2, th, tw, cpt, sec, 0};
+        if (!rc && sec < best.seconds_per_application) best = prk_gb300_tuning{0, tma_shape ? 2 : 4, th, tw, cpt, sec, 0};
     }
     if (!rc && batch) {  // the batched kernel with the whole run in one launch
         double sec = 0.0;
         rc = time_batch(pattern, radius, m, dtype, 0, s, &sec);
         if (!rc && sec < best.seconds_per_application) best = prk_gb300_tuning{0, 3, th, tw, cpt, sec, 0};
     }
-    if (!rc && !batch && tma_shape) {  // the generic kernels, depth 1
+    if (!rc && !batch) {  // the generic kernels, depth 1
         double sec = 0.0;
         prk_gb300_config(PRK_CFG_KERNEL, 1);
         rc = time_run(pattern, radius, m, dtype, 0, s, &sec);

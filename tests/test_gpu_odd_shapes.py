@@ -1,0 +1,152 @@
+"""Fused runs on shapes the TMA tiles cannot take: n not a multiple of the vector width, or buffers
+that are not 16-byte aligned. These run on the plain-staged tile kernels (the tile loaded with plain
+loads, then evaluated by the TMA kernels' code, with the same exact routes): the results must equal
+the strict-order oracle bit for bit in FP64 and stay within the 1e-6 bound in FP32C, at every
+temporal depth and for whole runs, and match the generic kernels'."""
+import numpy as np
+import pytest
+
+import kernels_gb300 as kg
+from oracle import prk_oracle as po
+
+pytestmark = pytest.mark.gpu
+
+ALL = [(p, r) for p in (kg.STAR, kg.GRID) for r in range(1, 6)]
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint64)
+
+
+def misaligned(torch, n, dtype):
+    """in_a, in_b, out as views starting 8 bytes past a 16-byte boundary."""
+    if dtype == kg.FP64:
+        def one(shape):
+            flat = torch.zeros(int(np.prod(shape)) + 1, dtype=torch.float64, device="cuda")
+            return flat[1:].view(*shape)
+        return one((n, n)), one((n, n)), one((n, n))
+    def one32(shape):
+        flat = torch.zeros(int(np.prod(shape)) + 2, dtype=torch.float32, device="cuda")
+        return flat[2:].view(*shape)
+    return one32((n, n)), one32((n, n)), one32((n, n, 2))
+
+
+@pytest.mark.parametrize("pattern,r", ALL)
+@pytest.mark.parametrize("mode", ["depth1", "depth4", "whole", "tuned"])
+def test_odd_n_fp64_bit_exact(cuda, pattern, r, mode):
+    n, k = 203, 9
+    _, ref = po.run(pattern, r, n, k)
+    in_a, in_b, out = kg.alloc(n, kg.FP64)
+    kg.init(in_a, out)
+    kw = {"depth1": {}, "depth4": {"depth": 4}, "whole": {"whole": True}, "tuned": {"tuned": True}}[mode]
+    res = kg.run(pattern, r, k, in_a, in_b, out, **kw)
+    assert np.array_equal(bits(out.cpu().numpy()), bits(ref))
+    ii, jj = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    assert np.array_equal(res.final_in.cpu().numpy(), (ii + jj + k + 1).astype(np.float64))
+
+
+@pytest.mark.parametrize("pattern,r", [(kg.STAR, 2), (kg.GRID, 3), (kg.STAR, 5)])
+@pytest.mark.parametrize("dtype", [kg.FP64, kg.FP32C])
+@pytest.mark.parametrize("graph", [False, True])
+def test_misaligned_buffers(cuda, pattern, r, dtype, graph):
+    n, k = 128, 7
+    _, ref = po.run(pattern, r, n, k)
+    in_a, in_b, out = misaligned(cuda, n, dtype)
+    assert in_a.data_ptr() % 16 == 8
+    kg.init(in_a, out)
+    res = kg.run(pattern, r, k, in_a, in_b, out, graph=graph, depth=2)
+    got = out.cpu().numpy()
+    ii, jj = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    if dtype == kg.FP64:
+        assert np.array_equal(bits(got), bits(ref))
+    else:
+        g64 = got[..., 0].astype(np.float64) + got[..., 1].astype(np.float64)
+        inner = (slice(r, n - r), slice(r, n - r))
+        assert (np.abs(g64[inner] - ref[inner]) / np.abs(ref[inner])).max() <= 1e-6
+        assert np.all(g64[:r] == 0) and np.all(g64[n - r:] == 0)
+    want = (ii + jj + k + 1).astype(np.float64)
+    assert np.array_equal(res.final_in.cpu().numpy().astype(np.float64), want)
+    assert abs(kg.norm(r, out) - 2.0 * (k + 1)) <= 1e-8
+
+
+@pytest.mark.parametrize("n", [130, 1001])
+@pytest.mark.parametrize("depth", [1, 8])
+def test_ragged_fp32c_error_bound(cuda, n, depth):
+    """FP32C with n not a multiple of 4 (the FP32 vector width)."""
+    r, k = 2, 12
+    _, ref = po.run(kg.STAR, r, n, k)
+    in_a, in_b, out = kg.alloc(n, kg.FP32C)
+    kg.init(in_a, out)
+    res = kg.run(kg.STAR, r, k, in_a, in_b, out, depth=depth)
+    got = out.cpu().numpy()
+    g64 = got[..., 0].astype(np.float64) + got[..., 1].astype(np.float64)
+    inner = (slice(r, n - r), slice(r, n - r))
+    assert (np.abs(g64[inner] - ref[inner]) / np.abs(ref[inner])).max() <= 1e-6
+    ii, jj = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    assert np.array_equal(res.final_in.cpu().numpy(), (ii + jj + k + 1).astype(np.float32))
+
+
+def test_long_run(cuda):
+    """5000 applications on an odd n, one launch each and all in one launch: bit-exact."""
+    n, r, k = 61, 2, 5000
+    _, ref = po.run(kg.STAR, r, n, k)
+    in_a, in_b, out = kg.alloc(n, kg.FP64)
+    kg.init(in_a, out)
+    res = kg.run(kg.STAR, r, k, in_a, in_b, out)
+    assert np.array_equal(bits(out.cpu().numpy()), bits(ref))
+    ii, jj = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    assert np.array_equal(res.final_in.cpu().numpy(), (ii + jj + k + 1).astype(np.float64))
+    kg.init(in_a, out)
+    res = kg.run(kg.STAR, r, k, in_a, in_b, out, whole=True)
+    assert np.array_equal(bits(out.cpu().numpy()), bits(ref))
+    assert np.array_equal(res.final_in.cpu().numpy(), (ii + jj + k + 1).astype(np.float64))
+
+
+@pytest.mark.parametrize("pattern,r", [(kg.STAR, 1), (kg.GRID, 2), (kg.STAR, 4)])
+@pytest.mark.parametrize("dtype", [kg.FP64, kg.FP32C])
+def test_plain_tiles_match_generic(cuda, pattern, r, dtype):
+    """Same inputs through the plain-staged tiles and through the generic kernels: FP64 bit for
+    bit; FP32C each within the bound of the oracle."""
+    n, k = 301, 5
+    outs = []
+    for choice in (kg.KERNEL_AUTO, kg.KERNEL_GENERIC):
+        prev = kg.set_kernel(choice)
+        try:
+            in_a, in_b, out = kg.alloc(n, dtype)
+            kg.init(in_a, out)
+            kg.run(pattern, r, k, in_a, in_b, out)
+            outs.append(out.cpu().numpy())
+        finally:
+            kg.set_kernel(prev)
+    if dtype == kg.FP64:
+        assert np.array_equal(bits(outs[0]), bits(outs[1]))
+    else:
+        _, ref = po.run(pattern, r, n, k)
+        inner = (slice(r, n - r), slice(r, n - r))
+        for o in outs:
+            g = o[..., 0].astype(np.float64) + o[..., 1].astype(np.float64)
+            assert (np.abs(g[inner] - ref[inner]) / np.abs(ref[inner])).max() <= 1e-6
+
+
+def test_tuner_on_odd_n(cuda):
+    t = kg.tune(kg.STAR, 2, 203, kg.FP64, force=True)
+    assert t["kernel"] in ("plain", "generic") and t["depth"] in (0, 1, 2, 4, 8)
+
+
+def test_odd_n_random_fields(cuda):
+    """Arbitrary in and out on an odd n: the batched kernel's certification falls back to the
+    strict binary64 order where the fields are not whole numbers."""
+    n, r, k = 157, 3, 4
+    rng = np.random.default_rng(157)
+    a = rng.standard_normal((n, n)) * 1e3
+    o = rng.standard_normal((n, n))
+    in_a = cuda.from_numpy(a.copy()).cuda()
+    in_b = cuda.empty_like(in_a)
+    out = cuda.from_numpy(o.copy()).cuda()
+    res = kg.run(kg.STAR, r, k, in_a, in_b, out, depth=4)
+    cur = a.copy()
+    for _ in range(k + 1):
+        po.apply(kg.STAR, r, cur, o)
+        cur = cur + 1.0
+    assert np.array_equal(bits(out.cpu().numpy()), bits(o))
+    assert np.array_equal(bits(res.final_in.cpu().numpy()), bits(cur))

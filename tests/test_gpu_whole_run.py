@@ -127,9 +127,13 @@ def test_run_host_banded_fp32c(cuda, pattern, r):
 
 
 def test_whole_run_rejections(cuda):
-    in_a, in_b, out = kg.alloc(63, kg.FP64)  # odd n: not the TMA shape
-    with pytest.raises(kg.PrkError):
-        kg.run(kg.STAR, 2, 3, in_a, in_b, out, whole=True)
+    in_a, in_b, out = kg.alloc(63, kg.FP64)  # odd n: the generic kernels have no whole-run form
+    prev = kg.set_kernel(kg.KERNEL_GENERIC)
+    try:
+        with pytest.raises(kg.PrkError):
+            kg.run(kg.STAR, 2, 3, in_a, in_b, out, whole=True)
+    finally:
+        kg.set_kernel(prev)
     in_a, in_b, out = kg.alloc(64, kg.FP64)
     with pytest.raises(kg.PrkError):
         kg.run(kg.STAR, 2, 3, in_a, None, out, whole=True, unfused=True)
