@@ -53,14 +53,15 @@ extern "C" {
 #define PRK_RUN_GRAPH 1   /* capture the timed iteration loop in a CUDA graph and replay it */
 #define PRK_RUN_UNFUSED 2 /* reference structure: stencil kernel, then a separate in += 1 pass */
 /* Temporal depth d in {1, 2, 4, 8}: each launch applies d consecutive applications to a tile held
- * in shared memory (the fused form on TMA-eligible buffers; otherwise depth 1). */
+ * in shared memory (the fused form on the tile kernels; depth 1 for PRK_RUN_UNFUSED and the generic
+ * kernels). */
 #define PRK_RUN_DEPTH(d) ((d) << 8)
 /* Tall tiles: 64 rows per TMA tile (8 rows per thread) instead of 32 (4 per thread). */
 #define PRK_RUN_TALL 8
 /* All timed applications in one launch: every tile carries iterations 1..K in shared memory (in
  * evolves pointwise, so a tile needs only its own rows and the R-row halo of the initial in). The
- * results are those of K single applications. Needs the TMA shape (as prk_gb300_stencil_steps);
- * overrides PRK_RUN_DEPTH and the tuned depth. */
+ * results are those of K single applications. The fused form only, on the tile kernels (as
+ * prk_gb300_stencil_steps); overrides PRK_RUN_DEPTH and the tuned depth. */
 #define PRK_RUN_WHOLE 16
 
 /* One application of the stencil (replaces starR/gridR, stencil_openmp.hpp:1, stencil_cuda.hpp:1):
@@ -77,9 +78,11 @@ int prk_gb300_stencil(int pattern, int radius, int64_t n, int dtype, const void*
  * out += S(in) + S(in+1) + ... + S(in+steps-1) with out rounded after every application exactly as
  * `steps` single applications round it, and in_next = in + steps (each +1 rounded in turn). Every
  * application reads the in values and applies every tap; only the HBM round trips between them are
- * saved. in is not modified. Needs 16-byte-aligned buffers and n a multiple of 2 (PRK_FP64) or 4
- * (PRK_FP32C); otherwise PRK_ERR_ARG. No counterpart in the reference, whose loop always makes the
- * round trip (Cxx11/stencil-openmp.cc:197-219). */
+ * saved. in is not modified. The TMA tile kernels take 16-byte-aligned buffers with n a multiple of
+ * 2 (PRK_FP64) or 4 (PRK_FP32C); other shapes run on the plain-staged tile kernels and need buffers
+ * aligned to their element size (8 bytes for out and PRK_FP64 in, 4 for PRK_FP32C in), else
+ * PRK_ERR_ARG. No counterpart in the reference, whose loop always makes the round trip
+ * (Cxx11/stencil-openmp.cc:197-219). */
 int prk_gb300_stencil_steps(int pattern, int radius, int64_t n, int dtype, int steps, const void* in, void* in_next,
                             void* out, void* stream);
 
@@ -136,10 +139,11 @@ int prk_gb300_run_host(int pattern, int radius, int64_t n, int dtype, int iterat
  *   start at zero). Calls that overlap on the GPU, e.g. on two streams, race on it. */
 int prk_gb300_norm_noalloc(int radius, int64_t n, int dtype, const void* out, double* norm_dev, void* stream);
 
-/* Process-wide settings. PRK_CFG_KERNEL selects the stencil kernel family: 0 = automatic (the TMA
- * tile kernels for the fused form on 16-byte-aligned buffers with n a multiple of 2 (FP64) or 4
- * (FP32C), the generic kernels otherwise), 1 = generic kernels only, 2 = TMA kernels required (calls
- * that are not eligible fail with PRK_ERR_ARG). Returns the previous value, or a negative error. */
+/* Process-wide settings. PRK_CFG_KERNEL selects the stencil kernel family: 0 = automatic (for the
+ * fused form, the TMA tile kernels on 16-byte-aligned buffers with n a multiple of 2 (FP64) or 4
+ * (FP32C) and the plain-staged tile kernels on other shapes; the generic kernels for the form
+ * without in_next), 1 = generic kernels only, 2 = TMA kernels required (calls that are not
+ * eligible fail with PRK_ERR_ARG). Returns the previous value, or a negative error. */
 #define PRK_CFG_KERNEL 1
 int prk_gb300_config(int key, int value);
 

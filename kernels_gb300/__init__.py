@@ -110,7 +110,8 @@ def apply(pattern: int, radius: int, in_, out, in_next=None, stream=None) -> Non
 
 def apply_steps(pattern: int, radius: int, steps: int, in_, out, in_next, stream=None) -> None:
     """`steps` (1, 2, 4 or 8) fused applications in one launch: out accumulates every application,
-    in_next = in + steps. Requires the TMA-eligible layout (16-byte alignment, n % 2 or n % 4)."""
+    in_next = in + steps. Any n; buffers aligned to their element size (the TMA tiles where the
+    layout allows them, the plain-staged tiles otherwise)."""
     n = _n_of(in_)
     dt = dtype_of(in_)
     _check_out(out, n, dt)

@@ -1,24 +1,19 @@
-// Instantiations of the batched kernel for fp32c storage, temporal depths 1, 2, 4, 8 and run-time depth.
+// The batched kernel for fp32c storage: the dispatch over temporal depths, and the instantiations
+// for depths 1, 2 and 4. Depth 8 and the run-time depth are in batch_fp32c_deep.cu.
 #include "batch_kernel.cuh"
 
 namespace prk {
 namespace batch {
 
+PRK_BATCH_INSTANTIATE(FP32C, 1)
+PRK_BATCH_INSTANTIATE(FP32C, 2)
+PRK_BATCH_INSTANTIATE(FP32C, 4)
+PRK_BATCH_EXTERN(FP32C, 8)
+PRK_BATCH_EXTERN(FP32C, 0)
+
 cudaError_t launch_fp32c(int steps, const Launch& L) { return launch_depth<FP32C>(steps, L); }
 
-int ctas_per_sm_fp32c(int steps)
-{
-    int b = 0;
-    cudaError_t e = cudaErrorInvalidValue;
-    switch (steps) {
-    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<FP32C, 1>, tile::THREADS, Layout<FP32C>::SMEM); break;
-    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<FP32C, 2>, tile::THREADS, Layout<FP32C>::SMEM); break;
-    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<FP32C, 4>, tile::THREADS, Layout<FP32C>::SMEM); break;
-    case 8: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<FP32C, 8>, tile::THREADS, Layout<FP32C>::SMEM); break;
-    case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<FP32C, 0>, tile::THREADS, Layout<FP32C>::SMEM); break;
-    }
-    return e == cudaSuccess ? b : 0;
-}
+int ctas_per_sm_fp32c(int steps) { return ctas_per_sm_depth<FP32C>(steps); }
 
 }  // namespace batch
 }  // namespace prk

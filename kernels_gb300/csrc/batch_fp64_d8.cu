@@ -1,0 +1,10 @@
+// The batched kernel for fp64 storage at temporal depth 8.
+#include "batch_kernel.cuh"
+
+namespace prk {
+namespace batch {
+
+PRK_BATCH_INSTANTIATE(FP64, 8)
+
+}  // namespace batch
+}  // namespace prk

@@ -141,6 +141,24 @@ cudaError_t launch(const Launch& L)
     return cudaGetLastError();
 }
 
+// Resident CTAs per SM of k_batch<DT, STEPS> (occupancy query; 0 on failure).
+template <int DT, int STEPS>
+int ctas_per_sm()
+{
+    int b = 0;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<DT, STEPS>, tile::THREADS, Layout<DT>::SMEM) == cudaSuccess
+               ? b : 0;
+}
+
+// Each (form, depth) pair is instantiated in one translation unit (batch_fp64*.cu, batch_fp32c*.cu)
+// so that the build compiles them in parallel; the dispatching units declare them with this.
+#define PRK_BATCH_EXTERN(DT, S)                                  \
+    extern template cudaError_t launch<DT, S>(const Launch& L); \
+    extern template int ctas_per_sm<DT, S>();
+#define PRK_BATCH_INSTANTIATE(DT, S)                      \
+    template cudaError_t launch<DT, S>(const Launch& L); \
+    template int ctas_per_sm<DT, S>();
+
 template <int DT>
 cudaError_t launch_depth(int steps, const Launch& L)
 {
@@ -152,6 +170,19 @@ cudaError_t launch_depth(int steps, const Launch& L)
     case 0: return launch<DT, 0>(L);
     }
     return cudaErrorInvalidValue;
+}
+
+template <int DT>
+int ctas_per_sm_depth(int steps)
+{
+    switch (steps) {
+    case 1: return ctas_per_sm<DT, 1>();
+    case 2: return ctas_per_sm<DT, 2>();
+    case 4: return ctas_per_sm<DT, 4>();
+    case 8: return ctas_per_sm<DT, 8>();
+    case 0: return ctas_per_sm<DT, 0>();
+    }
+    return 0;
 }
 
 // Per-form entry points (batch_fp64.cu, batch_fp32c.cu).

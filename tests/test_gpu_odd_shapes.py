@@ -150,3 +150,34 @@ def test_odd_n_random_fields(cuda):
         cur = cur + 1.0
     assert np.array_equal(bits(out.cpu().numpy()), bits(o))
     assert np.array_equal(bits(res.final_in.cpu().numpy()), bits(cur))
+
+
+@pytest.mark.parametrize("pattern,r", [(kg.STAR, 1), (kg.STAR, 2), (kg.GRID, 1), (kg.STAR, 3), (kg.GRID, 5)])
+@pytest.mark.parametrize("steps", [1, 2, 8])
+@pytest.mark.parametrize("kind", ["small_int", "dyadic", "wide_int", "random"])
+def test_apply_steps_odd_n(cuda, pattern, r, steps, kind):
+    """prk_gb300_stencil_steps on an odd n, each exact route (FP32, integer, whole-number products,
+    strict): the bits of `steps` single applications."""
+    n = 157
+    rng = np.random.default_rng(steps * 100 + r + len(kind))
+    if kind == "small_int":
+        a = rng.integers(-2**19, 2**19, (n, n)).astype(np.float64)
+    elif kind == "dyadic":
+        a = rng.integers(-2**20, 2**20, (n, n)) * 2.0 ** -9
+    elif kind == "wide_int":
+        a = rng.integers(-2**40, 2**40, (n, n)).astype(np.float64)
+    else:
+        a = rng.standard_normal((n, n)) * np.exp2(rng.integers(-10, 10, (n, n)))
+    o = rng.standard_normal((n, n))
+    want_in, want_out = a.copy(), o.copy()
+    for _ in range(steps):
+        po.apply(pattern, r, want_in, want_out)
+        want_in = want_in + 1.0
+    in_ = cuda.from_numpy(a).cuda()
+    out = cuda.from_numpy(o.copy()).cuda()
+    nxt = cuda.empty_like(in_)
+    kg.apply_steps(pattern, r, steps, in_, out, nxt)
+    kg.status()
+    assert np.array_equal(bits(out.cpu().numpy()), bits(want_out))
+    assert np.array_equal(bits(nxt.cpu().numpy()), bits(want_in))
+    assert np.array_equal(in_.cpu().numpy(), a)
