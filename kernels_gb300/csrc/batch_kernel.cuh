@@ -47,19 +47,15 @@ struct Layout {
     static constexpr int SMEM = RED_OFF + tile::WARPS * 8;
 };
 
-// One work item: load the tile of grid g at `parity`, then evaluate it.
-template <int P, int R, int DT, int STEPS>
-__device__ __forceinline__ void item(unsigned char* smem, int* s_red, const GridDesc& g, int64_t t, int parity,
-                                     int depth)
+// Stage the `in` tile at (i0, j0) with its halo in shared memory: coalesced plain loads, zero
+// outside the grid, all loads issued before the first shared-memory store.
+template <int R, int DT>
+__device__ __forceinline__ void stage_tile(unsigned char* smem, const void* in_v, int64_t n, int64_t i0, int64_t j0)
 {
     using G = tile::Geo<DT, R>;
-    using C = tile::Cfg<DT>;
-    using T = typename C::T;
+    using T = typename tile::Cfg<DT>::T;
     constexpr int PER = (G::ELEMS + tile::THREADS - 1) / tile::THREADS;
-    const int64_t n = g.n;
-    const int64_t i0 = (t / g.tiles_x) * C::TH;
-    const int64_t j0 = (t % g.tiles_x) * C::TW;
-    const T* __restrict__ in = static_cast<const T*>(g.in[parity]);
+    const T* __restrict__ in = static_cast<const T*>(in_v);
     T* s_in = reinterpret_cast<T*>(smem);
     T v[PER];
 #pragma unroll
@@ -75,6 +71,18 @@ __device__ __forceinline__ void item(unsigned char* smem, int* s_red, const Grid
         if (idx < G::ELEMS) s_in[idx] = v[q];
     }
     __syncthreads();
+}
+
+// One work item: load the tile of grid g at `parity`, then evaluate it.
+template <int P, int R, int DT, int STEPS>
+__device__ __forceinline__ void item(unsigned char* smem, int* s_red, const GridDesc& g, int64_t t, int parity,
+                                     int depth)
+{
+    using C = tile::Cfg<DT>;
+    const int64_t n = g.n;
+    const int64_t i0 = (t / g.tiles_x) * C::TH;
+    const int64_t j0 = (t % g.tiles_x) * C::TW;
+    stage_tile<R, DT>(smem, g.in[parity], n, i0, j0);
     tile::process_tile<P, R, DT, STEPS, true>(smem, s_red, i0, j0, n, tile::tile_has_out(i0, j0, n, R, C::TW, C::TH),
                                                g.in[parity ^ 1], g.out, g.vec_ok != 0, depth);
 }

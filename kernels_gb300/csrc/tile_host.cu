@@ -106,23 +106,8 @@ bool plain_eligible(const StencilCall& c)
 cudaError_t launch_stencil_plain(const StencilCall& c, int depth)
 {
     if (depth < 1 || !plain_eligible(c)) return cudaErrorInvalidValue;
-    using CF = tile::Cfg<FP64>;
-    using CC = tile::Cfg<FP32C>;
-    batch::GridDesc g{};
-    g.n = c.n;
-    g.in[0] = const_cast<void*>(c.in);
-    g.in[1] = c.in_next;
-    g.out = c.out;
-    g.pattern = c.pattern;
-    g.R = c.R;
-    const int tw = c.dtype == FP64 ? CF::TW : CC::TW;
-    const int th = c.dtype == FP64 ? CF::TH : CC::TH;
-    g.tiles_x = static_cast<int>((c.n + tw - 1) / tw);
-    g.tiles = ((c.n + th - 1) / th) * g.tiles_x;
-    g.vec_ok = 0;
-    const int steps = depth == 1 ? 1 : 0;
-    return c.dtype == FP64 ? plain::launch_fp64(c.pattern, c.R, steps, g, depth, c.stream)
-                           : plain::launch_fp32c(c.pattern, c.R, steps, g, depth, c.stream);
+    const plain::Args a{c.in, c.in_next, c.out, c.n, depth, c.stream};
+    return c.dtype == FP64 ? plain::launch_fp64(c.pattern, c.R, a) : plain::launch_fp32c(c.pattern, c.R, a);
 }
 
 cudaError_t launch_stencil_tma_band(const StencilCall& c, int depth, int64_t row0, int64_t rows, unsigned* status)

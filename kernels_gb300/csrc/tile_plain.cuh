@@ -21,39 +21,53 @@ struct Smem {
     static constexpr int BYTES = RED_OFF + tile::WARPS * 8;
 };
 
-// g.in[0] is `in`, g.in[1] is in_next; blockIdx = (tile column, tile row).
+// blockIdx = (tile column, tile row). The evaluation is compiled for one-by-one stores only (the
+// shapes here never allow the 16-byte vectors).
 template <int P, int R, int DT, int STEPS>
 __global__ void __launch_bounds__(tile::THREADS, tile::min_blocks<P, R, DT, STEPS, tile::TH_DEFAULT>())
-    k_stencil_plain(const batch::GridDesc g, const int depth)
+    k_stencil_plain(const void* __restrict__ in, void* __restrict__ in_next, void* __restrict__ out, const int64_t n,
+                    const int depth)
 {
+    using C = tile::Cfg<DT>;
     extern __shared__ __align__(128) unsigned char smem[];
     int* s_red = reinterpret_cast<int*>(smem + Smem<DT, R>::RED_OFF);
-    const int64_t t = static_cast<int64_t>(blockIdx.y) * g.tiles_x + blockIdx.x;
-    batch::item<P, R, DT, STEPS>(smem, s_red, g, t, 0, depth);
+    const int64_t i0 = static_cast<int64_t>(blockIdx.y) * C::TH;
+    const int64_t j0 = static_cast<int64_t>(blockIdx.x) * C::TW;
+    batch::stage_tile<R, DT>(smem, in, n, i0, j0);
+    tile::process_tile<P, R, DT, STEPS, true>(smem, s_red, i0, j0, n, tile::tile_has_out(i0, j0, n, R, C::TW, C::TH),
+                                               in_next, out, false, depth);
 }
 
+// The arguments of one launch: `depth` applications from in into in_next, accumulating into out.
+struct Args {
+    const void* in;
+    void* in_next;
+    void* out;
+    int64_t n;
+    int depth;
+    cudaStream_t stream;
+};
+
 template <int P, int R, int DT, int STEPS>
-cudaError_t launch(const batch::GridDesc& g, int depth, cudaStream_t s)
+cudaError_t launch(const Args& a)
 {
     using C = tile::Cfg<DT>;
     constexpr int SM = Smem<DT, R>::BYTES;
     if (cudaError_t e = cudaFuncSetAttribute(k_stencil_plain<P, R, DT, STEPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM))
         return e;
-    const int64_t ty = (g.n + C::TH - 1) / C::TH;
-    if (ty > 65535 || (STEPS == 0 && depth < 1)) return cudaErrorInvalidValue;
-    const dim3 grid(static_cast<unsigned>(g.tiles_x), static_cast<unsigned>(ty));
-    k_stencil_plain<P, R, DT, STEPS><<<grid, tile::THREADS, SM, s>>>(g, depth);
+    const int64_t tx = (a.n + C::TW - 1) / C::TW, ty = (a.n + C::TH - 1) / C::TH;
+    if (ty > 65535 || a.depth < 1) return cudaErrorInvalidValue;
+    const dim3 grid(static_cast<unsigned>(tx), static_cast<unsigned>(ty));
+    k_stencil_plain<P, R, DT, STEPS><<<grid, tile::THREADS, SM, a.stream>>>(a.in, a.in_next, a.out, a.n, a.depth);
     return cudaGetLastError();
 }
 
-// One application (steps = 1) or `depth` applications in one launch (steps = 0).
+// One application (depth 1: the STEPS = 1 kernel) or `depth` applications in one launch (STEPS = 0).
 template <int DT>
-cudaError_t launch_form(int pattern, int R, int steps, const batch::GridDesc& g, int depth, cudaStream_t s)
+cudaError_t launch_form(int pattern, int R, const Args& a)
 {
-#define PRK_PLAIN(PP, RR)                                                                    \
-    case RR:                                                                                 \
-        return steps == 1 ? launch<PP, RR, DT, 1>(g, 1, s) : launch<PP, RR, DT, 0>(g, depth, s);
-    if (steps != 0 && steps != 1) return cudaErrorInvalidValue;
+#define PRK_PLAIN(PP, RR) \
+    case RR: return a.depth == 1 ? launch<PP, RR, DT, 1>(a) : launch<PP, RR, DT, 0>(a);
     if (pattern == STAR) {
         switch (R) { PRK_PLAIN(STAR, 1) PRK_PLAIN(STAR, 2) PRK_PLAIN(STAR, 3) PRK_PLAIN(STAR, 4) PRK_PLAIN(STAR, 5) }
     } else {
@@ -64,8 +78,8 @@ cudaError_t launch_form(int pattern, int R, int steps, const batch::GridDesc& g,
 }
 
 // Per-form entry points (tile_plain_fp64.cu, tile_plain_fp32c.cu).
-cudaError_t launch_fp64(int pattern, int R, int steps, const batch::GridDesc& g, int depth, cudaStream_t s);
-cudaError_t launch_fp32c(int pattern, int R, int steps, const batch::GridDesc& g, int depth, cudaStream_t s);
+cudaError_t launch_fp64(int pattern, int R, const Args& a);
+cudaError_t launch_fp32c(int pattern, int R, const Args& a);
 
 }  // namespace plain
 }  // namespace prk

@@ -5,10 +5,7 @@
 namespace prk {
 namespace plain {
 
-cudaError_t launch_fp64(int pattern, int R, int steps, const batch::GridDesc& g, int depth, cudaStream_t s)
-{
-    return launch_form<FP64>(pattern, R, steps, g, depth, s);
-}
+cudaError_t launch_fp64(int pattern, int R, const Args& a) { return launch_form<FP64>(pattern, R, a); }
 
 }  // namespace plain
 }  // namespace prk
