@@ -48,22 +48,38 @@ struct Layout {
 };
 
 // Stage the `in` tile at (i0, j0) with its halo in shared memory: coalesced plain loads, zero
-// outside the grid, all loads issued before the first shared-memory store.
+// outside the grid, all loads issued before the first shared-memory store. Thread t takes elements
+// t, t + THREADS, ... of the row-major tile; its row, column and grid offset advance by constants
+// from one element to the next (one division per thread, none per element).
 template <int R, int DT>
 __device__ __forceinline__ void stage_tile(unsigned char* smem, const void* in_v, int64_t n, int64_t i0, int64_t j0)
 {
     using G = tile::Geo<DT, R>;
     using T = typename tile::Cfg<DT>::T;
     constexpr int PER = (G::ELEMS + tile::THREADS - 1) / tile::THREADS;
+    constexpr int DR = tile::THREADS / G::SW, DC = tile::THREADS % G::SW;
     const T* __restrict__ in = static_cast<const T*>(in_v);
     T* s_in = reinterpret_cast<T*>(smem);
+    const uint32_t un = static_cast<uint32_t>(n);  // n <= NMAX < 2^31
+    int r = threadIdx.x / G::SW, c = threadIdx.x - (threadIdx.x / G::SW) * G::SW;
+    int gi = static_cast<int>(i0) - R + r, gj = static_cast<int>(j0) - G::RA + c;
+    int64_t off = static_cast<int64_t>(gi) * n + gj;
     T v[PER];
 #pragma unroll
     for (int q = 0; q < PER; ++q) {  // all loads first, then the shared-memory stores
         const int idx = threadIdx.x + q * tile::THREADS;
-        const int r = idx / G::SW, c = idx - (idx / G::SW) * G::SW;
-        const int64_t gi = i0 - R + r, gj = j0 - G::RA + c;
-        v[q] = (idx < G::ELEMS && gi >= 0 && gi < n && gj >= 0 && gj < n) ? in[gi * n + gj] : T(0);
+        const bool ok = (q + 1) * tile::THREADS <= G::ELEMS || idx < G::ELEMS;
+        v[q] = (ok && static_cast<uint32_t>(gi) < un && static_cast<uint32_t>(gj) < un) ? in[off] : T(0);
+        c += DC;
+        gi += DR;
+        gj += DC;
+        off += DR * n + DC;
+        if (c >= G::SW) {
+            c -= G::SW;
+            gi += 1;
+            gj -= G::SW;
+            off += n - G::SW;
+        }
     }
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
