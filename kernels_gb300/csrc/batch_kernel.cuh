@@ -99,7 +99,7 @@ __device__ __forceinline__ void item(unsigned char* smem, int* s_red, const Grid
     const int64_t i0 = (t / g.tiles_x) * C::TH;
     const int64_t j0 = (t % g.tiles_x) * C::TW;
     stage_tile<R, DT>(smem, g.in[parity], n, i0, j0);
-    tile::process_tile<P, R, DT, STEPS, true>(smem, s_red, i0, j0, n, tile::tile_has_out(i0, j0, n, R, C::TW, C::TH),
+    tile::process_tile<P, R, DT, STEPS, tile::OUT_HBM>(smem, s_red, i0, j0, n, tile::tile_has_out(i0, j0, n, R, C::TW, C::TH),
                                                g.in[parity ^ 1], g.out, g.vec_ok != 0, depth);
 }
 

@@ -702,12 +702,17 @@ __device__ __forceinline__ bool tile_has_out(int64_t i0, int64_t j0, int64_t n, 
     return (i0 + th > R) && (i0 < n - R) && (j0 + tw > R) && (j0 < n - R);
 }
 
+// Where process_tile finds `out`: the out tile loaded into shared memory next to `in` (TMA path), or
+// HBM, read in the evaluation row by row (batched path) or with every row's words requested before
+// the first row is evaluated (plain-staged path; used for the FP64 power-of-two stencils at one
+// application, where it measured faster, and like OUT_HBM otherwise).
+constexpr int OUT_SMEM = 0, OUT_HBM = 1, OUT_HBM_AHEAD = 2;
+
 // Evaluate one tile whose `in` (with halo) is in shared memory: STEPS applications (`depth` when
-// STEPS = 0), then in_next and out to HBM. GLOBAL_OUT = false: the out tile was loaded into shared
-// memory next to `in` (TMA path); true: out is read from HBM here (batched path). vec_ok: rows are
-// 16-byte aligned and n is a multiple of CPT, so a thread's CPT points move as one vector;
-// otherwise they move one by one.
-template <int P, int R, int DT, int STEPS, bool GLOBAL_OUT = false, int TH_ = 32>
+// STEPS = 0), then in_next and out to HBM, with out read from OUT_SRC. vec_ok: rows are 16-byte
+// aligned and n is a multiple of CPT, so a thread's CPT points move as one vector; otherwise they
+// move one by one.
+template <int P, int R, int DT, int STEPS, int OUT_SRC = OUT_SMEM, int TH_ = 32>
 __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, int64_t i0, int64_t j0, int64_t n,
                                              bool has_out, void* __restrict__ in_next_v, void* __restrict__ out_v,
                                              bool vec_ok = true, int depth = 0)
@@ -729,7 +734,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
     const bool cols_interior = gj >= R && gj + CPT <= n - R;
     // the out word of point (r, c0 + k), from the smem out tile or from HBM
     auto load_out = [&](int r, int k) -> uint64_t {
-        if constexpr (GLOBAL_OUT) {
+        if constexpr (OUT_SRC != OUT_SMEM) {
             return gj + k < n ? static_cast<const uint64_t*>(out_v)[(i0 + r) * n + gj + k] : 0ull;
         } else {
             return o_tile[r * C::TW + c0 + k];
@@ -984,7 +989,21 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
     };
 
     if constexpr (STEPS == 1) {
-        // one pass: each row's new out and in_next leave as soon as they are computed
+        // one pass: each row's new out and in_next leave as soon as they are computed. OUT_HBM_AHEAD:
+        // every row's out words are requested first, so that their latencies overlap instead of
+        // stalling each row in turn.
+        constexpr bool PRELOAD = OUT_SRC == OUT_HBM_AHEAD && EXACT;
+        uint64_t o_pre[PRELOAD ? ROWS : 1][CPT];
+        if constexpr (PRELOAD) {
+#pragma unroll
+            for (int rr = 0; rr < ROWS; ++rr) {
+                const int r = warp * ROWS + rr;
+                const int64_t gi = i0 + r;
+                const bool row_out = col_ok && gi < n && has_out && gi >= R && gi < n - R;
+#pragma unroll
+                for (int k = 0; k < CPT; ++k) o_pre[rr][k] = row_out ? load_out(r, k) : 0ull;
+            }
+        }
 #pragma unroll
         for (int rr = 0; rr < ROWS; ++rr) {
             const int r = warp * ROWS + rr;
@@ -994,7 +1013,12 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
             uint64_t o[CPT];
             if (row_out) {
 #pragma unroll
-                for (int k = 0; k < CPT; ++k) o[k] = load_out(r, k);
+                for (int k = 0; k < CPT; ++k) {
+                    if constexpr (PRELOAD)
+                        o[k] = o_pre[rr][k];
+                    else
+                        o[k] = load_out(r, k);
+                }
                 apply_row(r, o);
             }
             store_row(r, o, row_out);
@@ -1199,7 +1223,7 @@ __global__ void __launch_bounds__(THREADS, min_blocks<P, R, DT, STEPS, TH_>())
         mbar_wait_bounded(bar, 0);  // let the copies land before the CTA's shared memory is released
         return;
     }
-    process_tile<P, R, DT, STEPS, false, TH_>(smem, s_red, i0, j0, n, has_out, in_next_v, out_v, true, depth);
+    process_tile<P, R, DT, STEPS, OUT_SMEM, TH_>(smem, s_red, i0, j0, n, has_out, in_next_v, out_v, true, depth);
 }
 
 template <int P, int R, int DT, int STEPS, int TH_>

@@ -181,3 +181,26 @@ def test_apply_steps_odd_n(cuda, pattern, r, steps, kind):
     assert np.array_equal(bits(out.cpu().numpy()), bits(want_out))
     assert np.array_equal(bits(nxt.cpu().numpy()), bits(want_in))
     assert np.array_equal(in_.cpu().numpy(), a)
+
+
+@pytest.mark.parametrize("pattern,r", [(kg.STAR, 2), (kg.GRID, 3)])
+@pytest.mark.parametrize("mode", ["depth1", "whole"])
+def test_full_size_odd_n(cuda, pattern, r, mode):
+    """n=16383 (odd, the headline size less one), 100 iterations, FP64: norm check, sampled points
+    against the per-point oracle (bit-exact), and the final `in` field."""
+    n, K = 16383, 100
+    in_a, in_b, out = kg.alloc(n, kg.FP64)
+    kg.init(in_a, out)
+    res = kg.run(pattern, r, K, in_a, in_b, out, whole=mode == "whole")
+    assert abs(kg.norm(r, out) - 2.0 * (K + 1)) <= 1e-8
+    rng = np.random.default_rng(16383 + r)
+    pts = [(r, r), (n - r - 1, n - r - 1), (r, n - r - 1), (n - r - 1, r), (8191, 8192)] + \
+          [tuple(int(x) for x in rng.integers(r, n - r, 2)) for _ in range(40)]
+    idx = cuda.tensor([i * n + j for i, j in pts], device="cuda")
+    got = out.reshape(-1)[idx].cpu().numpy()
+    for (i, j), v in zip(pts, got):
+        assert v == po.point(pattern, r, n, K + 1, i, j), (i, j)
+    fin = res.final_in.reshape(-1)[idx].cpu().numpy()
+    assert all(f == i + j + K + 1 for (i, j), f in zip(pts, fin))
+    del in_a, in_b, out, res
+    cuda.cuda.empty_cache()
