@@ -108,10 +108,12 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
 
 /* A whole PRK run from host memory, the way Cxx11/stencil-cuda.cu drives it (:193-226): copies
  * h_in and h_out to the device, runs iterations+1 fused applications, copies out (and the final in,
- * when h_in_final != NULL) back, and computes the norm. For the TMA shape (n a multiple of 2 for
- * PRK_FP64, 4 for PRK_FP32C) the grid goes in bands of rows: each band's copies in, its one launch
- * carrying all iterations+1 applications, and its copies back overlap those of the other bands.
- * Other shapes copy in, run with the autotuner's choice (PRK_RUN_TUNED) and copy back. Its device
+ * when h_in_final != NULL) back, and computes the norm. The grid goes in bands of rows: each band's
+ * copies in, its one launch carrying all iterations+1 applications (TMA tiles, or plain-staged
+ * tiles for an n the TMA tiles cannot take), and its copies back overlap those of the other bands.
+ * With PRK_CFG_KERNEL 1 (generic kernels only) it copies in, runs with the autotuner's choice
+ * (PRK_RUN_TUNED) and copies back; with 2 (TMA required) an n the TMA tiles cannot take is
+ * PRK_ERR_ARG. Its device
  * buffers and streams are allocated on first use and kept for later calls (the buffers grown when
  * a larger grid comes); prk_gb300_release frees them. Calls are serialised process-wide.
  * *elapsed_s (optional) is the whole call's wall time including the copies; *kernel_s (optional)

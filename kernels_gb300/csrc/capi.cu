@@ -288,7 +288,7 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
         prk_gb300_tuning t{};
         if (int rc = prk_gb300_tune(pattern, radius, n, dtype, 0, &t)) return rc;
         depth = t.depth > 0 ? t.depth : 1;
-        whole = t.depth == 0;
+        whole = t.depth == 0 && g_kernel_choice != 1;  // the generic kernels run one application per launch
         tuned_generic = t.kernel == 1;
         if (!tuned_generic) rows = t.tile_rows;
     }
@@ -492,7 +492,10 @@ int run_host_banded(HostWorkspace& ws, int pattern, int radius, int64_t n, int d
         PRK_CUDA(cudaStreamWaitEvent(st, landed.ev[b + 1 < nb ? b + 1 : b], 0), "cudaStreamWaitEvent");
         if (b == 0) PRK_CUDA(cudaEventRecord(span.ev[0], st), "cudaEventRecord");
         prk::StencilCall c{pattern, radius, n, dtype, d_in, d_fin, d_out, st};
-        PRK_CUDA(prk::launch_stencil_tma_band(c, apps, r0, rows, sc.status), "band launch (TMA tiles)");
+        if (prk::tma_eligible(c))
+            PRK_CUDA(prk::launch_stencil_tma_band(c, apps, r0, rows, sc.status), "band launch (TMA tiles)");
+        else
+            PRK_CUDA(prk::launch_stencil_plain(c, apps, r0, rows), "band launch (plain-staged tiles)");
         PRK_CUDA(cudaEventRecord(done.ev[b], st), "cudaEventRecord");
         PRK_CUDA(cudaStreamWaitEvent(s_out, done.ev[b], 0), "cudaStreamWaitEvent");
         PRK_CUDA(cudaMemcpyAsync(ho + r0 * n * 8, d_out + r0 * n * 8, rows * n * 8, cudaMemcpyDeviceToHost, s_out),
@@ -560,7 +563,8 @@ int prk_gb300_run_host(int pattern, int radius, int64_t n, int dtype, int iterat
         void** d = ws.d;
         {
             prk::StencilCall probe{pattern, radius, n, dtype, d[0], d[1], d[2], nullptr};
-            if (g_kernel_choice != 1 && prk::tma_eligible(probe)) {  // iteration 0 plus `iterations`
+            const bool tiles = prk::tma_eligible(probe) || (g_kernel_choice == 0 && prk::plain_eligible(probe));
+            if (g_kernel_choice != 1 && tiles) {  // iteration 0 plus `iterations`
                 rc = run_host_banded(ws, pattern, radius, n, dtype, iterations + 1, h_in, h_out, h_in_final, norm, kernel_s);
                 break;
             }

@@ -44,9 +44,11 @@ cudaError_t launch_stencil_tma_band(const StencilCall& c, int depth, int64_t row
 
 // tile_plain_*.cu: the fused form on shapes the TMA kernels cannot take (any n, buffers aligned to
 // their element size); the tile staged with plain loads, then evaluated as in the TMA kernels.
-// `depth` applications in one launch (1 for one application per launch).
+// `depth` applications in one launch (1 for one application per launch), over the tiles of grid
+// rows [row0, row0 + rows) (row0 a multiple of 32; rows = 0: to the last row), reading `in` rows
+// row0 - R .. row0 + rows + R - 1 as launch_stencil_tma_band does.
 bool plain_eligible(const StencilCall& c);
-cudaError_t launch_stencil_plain(const StencilCall& c, int depth);
+cudaError_t launch_stencil_plain(const StencilCall& c, int depth, int64_t row0 = 0, int64_t rows = 0);
 
 // kernels_generic.cu: any n, any 8-byte-aligned pointers.
 cudaError_t launch_stencil_generic(const StencilCall& c);

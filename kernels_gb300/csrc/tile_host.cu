@@ -103,10 +103,10 @@ bool plain_eligible(const StencilCall& c)
     return al(c.in, e) && al(c.in_next, e) && al(c.out, 8);
 }
 
-cudaError_t launch_stencil_plain(const StencilCall& c, int depth)
+cudaError_t launch_stencil_plain(const StencilCall& c, int depth, int64_t row0, int64_t rows)
 {
     if (depth < 1 || !plain_eligible(c)) return cudaErrorInvalidValue;
-    const plain::Args a{c.in, c.in_next, c.out, c.n, depth, c.stream};
+    const plain::Args a{c.in, c.in_next, c.out, c.n, depth, c.stream, row0, rows};
     return c.dtype == FP64 ? plain::launch_fp64(c.pattern, c.R, a) : plain::launch_fp32c(c.pattern, c.R, a);
 }
 

@@ -3,8 +3,9 @@
 //
 // One CTA per tile, as in the TMA kernel, so that several tiles per SM are in flight at once. The
 // `in` tile and its halo are staged in shared memory with coalesced plain loads (zero outside the
-// grid), `out` is read from HBM in the evaluation, and the tile is then evaluated by the same code
-// as the TMA and batched kernels (stencil_tile.cuh): the same exact routes, the same certification.
+// grid), `out` is read from HBM by the evaluation (tile::OUT_HBM_AHEAD), and the tile is evaluated
+// by the same code as the TMA and batched kernels (stencil_tile.cuh): the same exact routes, the
+// same certification.
 // STEPS = 1 is one application per launch; STEPS = 0 takes the number of applications at run time
 // (any temporal depth, or a whole run).
 #pragma once
@@ -32,24 +33,26 @@ constexpr int plain_min_blocks()
     return DT == FP64 && pow2_weights(P, R) && STEPS == 1 && b > 5 ? 5 : b;
 }
 
-// blockIdx = (tile column, tile row). The evaluation is compiled for one-by-one stores only (the
-// shapes here never allow the 16-byte vectors).
+// blockIdx = (tile column, tile row counted from row0). The evaluation is compiled for one-by-one
+// stores only (the shapes here never allow the 16-byte vectors).
 template <int P, int R, int DT, int STEPS>
 __global__ void __launch_bounds__(tile::THREADS, plain_min_blocks<P, R, DT, STEPS>())
     k_stencil_plain(const void* __restrict__ in, void* __restrict__ in_next, void* __restrict__ out, const int64_t n,
-                    const int depth)
+                    const int depth, const int64_t row0)
 {
     using C = tile::Cfg<DT>;
     extern __shared__ __align__(128) unsigned char smem[];
     int* s_red = reinterpret_cast<int*>(smem + Smem<DT, R>::RED_OFF);
-    const int64_t i0 = static_cast<int64_t>(blockIdx.y) * C::TH;
+    const int64_t i0 = row0 + static_cast<int64_t>(blockIdx.y) * C::TH;
     const int64_t j0 = static_cast<int64_t>(blockIdx.x) * C::TW;
+    const bool has_out = tile::tile_has_out(i0, j0, n, R, C::TW, C::TH);
     batch::stage_tile<R, DT>(smem, in, n, i0, j0);
-    tile::process_tile<P, R, DT, STEPS, tile::OUT_HBM_AHEAD>(smem, s_red, i0, j0, n, tile::tile_has_out(i0, j0, n, R, C::TW, C::TH),
-                                               in_next, out, false, depth);
+    tile::process_tile<P, R, DT, STEPS, tile::OUT_HBM_AHEAD>(smem, s_red, i0, j0, n, has_out, in_next, out, false, depth);
 }
 
-// The arguments of one launch: `depth` applications from in into in_next, accumulating into out.
+// The arguments of one launch: `depth` applications from in into in_next, accumulating into out,
+// over the tiles of grid rows [row0, row0 + rows) (row0 a multiple of the tile height; rows = 0:
+// to the last row).
 struct Args {
     const void* in;
     void* in_next;
@@ -57,6 +60,8 @@ struct Args {
     int64_t n;
     int depth;
     cudaStream_t stream;
+    int64_t row0;
+    int64_t rows;
 };
 
 template <int P, int R, int DT, int STEPS>
@@ -66,10 +71,12 @@ cudaError_t launch(const Args& a)
     constexpr int SM = Smem<DT, R>::BYTES;
     if (cudaError_t e = cudaFuncSetAttribute(k_stencil_plain<P, R, DT, STEPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM))
         return e;
-    const int64_t tx = (a.n + C::TW - 1) / C::TW, ty = (a.n + C::TH - 1) / C::TH;
-    if (ty > 65535 || a.depth < 1) return cudaErrorInvalidValue;
+    if (a.row0 < 0 || a.row0 % C::TH != 0 || a.row0 >= a.n || a.rows < 0 || a.depth < 1) return cudaErrorInvalidValue;
+    const int64_t rows = a.rows > 0 && a.rows < a.n - a.row0 ? a.rows : a.n - a.row0;
+    const int64_t tx = (a.n + C::TW - 1) / C::TW, ty = (rows + C::TH - 1) / C::TH;
+    if (ty > 65535) return cudaErrorInvalidValue;
     const dim3 grid(static_cast<unsigned>(tx), static_cast<unsigned>(ty));
-    k_stencil_plain<P, R, DT, STEPS><<<grid, tile::THREADS, SM, a.stream>>>(a.in, a.in_next, a.out, a.n, a.depth);
+    k_stencil_plain<P, R, DT, STEPS><<<grid, tile::THREADS, SM, a.stream>>>(a.in, a.in_next, a.out, a.n, a.depth, a.row0);
     return cudaGetLastError();
 }
 

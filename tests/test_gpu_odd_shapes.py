@@ -204,3 +204,56 @@ def test_full_size_odd_n(cuda, pattern, r, mode):
     assert all(f == i + j + K + 1 for (i, j), f in zip(pts, fin))
     del in_a, in_b, out, res
     cuda.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("n", [203, 1001])
+@pytest.mark.parametrize("dtype", [kg.FP64, kg.FP32C])
+@pytest.mark.parametrize("pattern,r", [(kg.STAR, 2), (kg.GRID, 3)])
+def test_run_host_odd_n_banded(cuda, n, dtype, pattern, r):
+    """prk_gb300_run_host on an odd n: bands of plain-staged tiles (n=1001: eight bands of 128 rows,
+    the last 105), each carrying every application, against the oracle and the generic kernels'
+    unbanded run."""
+    k = 7
+    _, ref = po.run(pattern, r, n, k)
+    ii, jj = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    if dtype == kg.FP64:
+        h_in = (ii + jj).astype(np.float64)
+        h_out = np.zeros((n, n))
+    else:
+        h_in = (ii + jj).astype(np.float32)
+        h_out = np.zeros((n, n, 2), np.float32)
+    h_fin = np.empty_like(h_in)
+    res = kg.run_host(pattern, r, k, h_in, h_out, h_fin)
+    inner = (slice(r, n - r), slice(r, n - r))
+    if dtype == kg.FP64:
+        assert np.array_equal(bits(h_out), bits(ref))
+    else:
+        got = h_out.astype(np.float64).sum(axis=-1)
+        assert (np.abs(got[inner] - ref[inner]) / np.abs(ref[inner])).max() <= 1e-6
+    assert np.array_equal(h_fin, h_in + h_in.dtype.type(k + 1))
+    assert abs(res["norm"] - 2.0 * (k + 1)) <= 1e-8
+    assert res["kernel_s"] > 0
+    prev = kg.set_kernel(kg.KERNEL_GENERIC)
+    try:
+        h_out2 = np.zeros_like(h_out)
+        kg.run_host(pattern, r, k, h_in, h_out2)
+    finally:
+        kg.set_kernel(prev)
+    if dtype == kg.FP64:
+        assert np.array_equal(bits(h_out2), bits(h_out))
+
+
+def test_tuned_run_with_generic_kernels_only(cuda):
+    """A tuned run while the generic kernels are selected process-wide: a cached choice of the whole
+    run in one launch (a tile-kernel form) falls back to one application per launch."""
+    n, r, k = 203, 2, 5
+    kg.tune(kg.STAR, r, n, kg.FP64)
+    _, ref = po.run(kg.STAR, r, n, k)
+    prev = kg.set_kernel(kg.KERNEL_GENERIC)
+    try:
+        in_a, in_b, out = kg.alloc(n, kg.FP64)
+        kg.init(in_a, out)
+        kg.run(kg.STAR, r, k, in_a, in_b, out, tuned=True)
+    finally:
+        kg.set_kernel(prev)
+    assert np.array_equal(bits(out.cpu().numpy()), bits(ref))
