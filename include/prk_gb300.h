@@ -145,7 +145,8 @@ int prk_gb300_norm_noalloc(int radius, int64_t n, int dtype, const void* out, do
  * fused form, the TMA tile kernels on 16-byte-aligned buffers with n a multiple of 2 (FP64) or 4
  * (FP32C) and the plain-staged tile kernels on other shapes; the generic kernels for the form
  * without in_next), 1 = generic kernels only, 2 = TMA kernels required (calls that are not
- * eligible fail with PRK_ERR_ARG). Returns the previous value, or a negative error. */
+ * eligible fail with PRK_ERR_ARG). Returns the previous value, or a negative error. Callable from
+ * any thread; it governs the calls that start after it returns. */
 #define PRK_CFG_KERNEL 1
 int prk_gb300_config(int key, int value);
 

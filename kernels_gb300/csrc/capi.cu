@@ -2,6 +2,7 @@
 // kernel launchers, the timed iteration loop and the host-buffer entry point. Errors are returned,
 // never raised: a negative PRK_ERR_* for a rejected call, a positive cudaError_t otherwise.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstdarg>
 #include <cstdio>
@@ -116,7 +117,8 @@ std::mutex g_host_mu;
 std::vector<HostWorkspace> g_host_ws;
 
 // Kernel selection: 0 = automatic (TMA tiles where eligible), 1 = generic only, 2 = TMA required.
-int g_kernel_choice = 0;
+// Atomic, so that prk_gb300_config may be called while other threads run stencils.
+std::atomic<int> g_kernel_choice{0};
 // Set for the duration of a tuned run whose tuning chose the generic kernels, or a tile height.
 thread_local bool t_force_generic = false;
 thread_local int t_tile_rows = 32;
@@ -187,9 +189,7 @@ int prk_gb300_config(int key, int value)
 {
     if (key == PRK_CFG_KERNEL) {
         if (value < 0 || value > 2) return fail(PRK_ERR_ARG, "PRK_CFG_KERNEL takes 0 (auto), 1 (generic) or 2 (TMA)");
-        const int old = g_kernel_choice;
-        g_kernel_choice = value;
-        return old;
+        return g_kernel_choice.exchange(value);
     }
     return fail(PRK_ERR_ARG, "unknown configuration key %d", key);
 }
