@@ -33,6 +33,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "GFLOP/s + HBM GB/s, star R=2 n=16384: FP64 vs FP32-comp (rel err<=1e-6)"
 N_DEFAULT, R_DEFAULT = 16384, 2
 PEAK_FALLBACK_GBS = 6800.0
+L2_BYTES = 129 * 2**20  # GB300's last-level cache, for the config's L2 note
 
 
 def algorithmic_bytes(n: int, r: int, fp64: bool) -> float:
@@ -162,7 +163,8 @@ def run_reference(args) -> None:
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * t / args.steps, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"PRK star stencil R={r}, n={n}, FP64, one application + in+=1 per step",
-                   "pattern": "star", "radius": r, "n": n, "l2": "inputs larger than L2"},
+                   "pattern": "star", "radius": r, "n": n,
+                   "l2": "inputs larger than L2" if 8 * n * n > L2_BYTES else "inputs within L2 (a small case)"},
         "hbm_gbs": round(algorithmic_bytes(n, r, True) * args.steps / t / 1e9, 2),
         "cpu_baseline": {"value": round(value, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port",
                          "sample": f"{args.steps} applications at n={n} (stencil-openmp loop restated in C, "
@@ -374,7 +376,9 @@ def run_gb300(args) -> None:
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"PRK star stencil R={r}, n={n}, FP64, one fused application (out += S(in), "
                                f"in_next = in + 1) per step", "pattern": "star", "radius": r, "n": n,
-                   "l2": "inputs larger than L2 (2.1 GB per array), no flush", "parallelism": f"replicas x{world}"},
+                   "l2": (f"inputs larger than L2 ({8 * n * n / 1e9:.1f} GB per array), no flush" if 8 * n * n > L2_BYTES
+                          else "inputs within L2 (a small case, not the benchmark)"),
+                   "parallelism": f"replicas x{world}"},
         "hbm_gbs": round(world * ach64, 2),
         "norm_check": norm_ok,
         "roofline": {"bound": "hbm", "achieved": round(ach64, 2), "peak": peak, "unit": "GB/s",
