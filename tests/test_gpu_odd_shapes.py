@@ -2,7 +2,7 @@
 that are not 16-byte aligned. These run on the plain-staged tile kernels (the tile loaded with plain
 loads, then evaluated by the TMA kernels' code, with the same exact routes): the results must equal
 the strict-order oracle bit for bit in FP64 and stay within the 1e-6 bound in FP32C, at every
-temporal depth and for whole runs, and match the generic kernels'."""
+temporal depth, for whole runs and for banded host-buffer runs, and match the generic kernels'."""
 import numpy as np
 import pytest
 
