@@ -6,7 +6,10 @@ stencil at 2.1 GB per array, the configuration the headline metric is quoted on.
 larger than the 129 MB L2, so no flush is needed between steps. The same workload is also measured
 in the FP32-compensated form (the "fp32c" key) with its relative error against the FP64 path, whose
 results are bit-identical to the reference's (the parity tests check that), and as the seeded
-256-grid batched configuration (the "batched" key).
+256-grid batched configuration (the "batched" key). The "grid2" key is the grid R=2 stencil on the
+same grid, FP64, with both of its ceilings (HBM and the binary64 add rate, measured in the run), and
+"gpu_comparator" times the reference's own CUDA stencil (Cxx11/stencil-cuda.cu built for sm_103a)
+on the headline grid, outside the timed region, when its cubin was built.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -174,6 +177,33 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def reference_cuda_rate(torch, kg, n: int, r: int, iterations: int = 20) -> dict | None:
+    """The reference's CUDA stencil (Cxx11/stencil-cuda.cu compiled for sm_103a into
+    oracle/_ref/stencil_cuda.cubin) driven as its own loop drives it (stencil kernel, add kernel and
+    a device synchronise per iteration, tile 32), star R at size n, beside the fused tile kernel on
+    the same grid. A baseline, timed outside this benchmark's timed region; None when the cubin was
+    not built."""
+    try:
+        from oracle import ref_cuda
+    except Exception:
+        return None
+    if not ref_cuda.available():
+        return None
+    idx = torch.arange(n, dtype=torch.float64, device="cuda")
+    d_in = (idx[:, None] + idx[None, :]).contiguous()
+    d_out = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    t_ref = ref_cuda.run("star", r, n, iterations, d_in.data_ptr(), d_out.data_ptr(), 32)
+    nrm_ref = kg.norm(r, d_out)
+    del d_in, d_out, idx
+    torch.cuda.empty_cache()
+    fl = kg.flops(kg.STAR, r, n) * iterations
+    return {"what": f"reference Cxx11/stencil-cuda.cu (device code compiled for sm_103a from the reference "
+                    f"sources), star R={r}, n={n}, {iterations} timed iterations, tile 32, its own loop",
+            "ms_per_iteration": round(t_ref / iterations * 1e3, 4), "gflops": round(fl / t_ref / 1e9, 3),
+            "norm_check": abs(nrm_ref - 2.0 * (iterations + 1)) <= 1e-8}
+
+
 def time_steps(torch, kg, pattern, r, bufs, out, steps, warmup, stream) -> tuple[float, int]:
     """W untimed + K timed fused applications on `stream`; returns (seconds, final parity)."""
     cur = 0
@@ -288,6 +318,46 @@ def run_gb300(args) -> None:
     del in_a, in_b, out
     torch.cuda.empty_cache()
 
+    # ---- grid R=2, the other half of the headline configuration, FP64, one application per launch ----
+    grid2 = None
+    if not args.no_grid:
+        in_a, in_b, out = kg.alloc(n, kg.FP64)
+        kg.init(in_a, out)
+        barrier()
+        g_steps = max(args.steps // 4, 5)
+        tg, _ = time_steps(torch, kg, kg.GRID, r, (in_a, in_b), out, g_steps, args.warmup, stream)
+        barrier()
+        tg = max_over_ranks(tg)
+        nrm_g = kg.norm(r, out)
+        del in_a, in_b, out
+        torch.cuda.empty_cache()
+        fl_g = kg.flops(kg.GRID, r, n)
+        per_g = tg / g_steps
+        bg = algorithmic_bytes(n, r, True)
+        t_hbm = bg / (hbm_peak()[0] * 1e9)
+        rate = kg.probe_dadd()
+        # the strict order's rounded binary64 adds: the chain's taps - 1 and the add into out
+        adds = 4 * r * r + 2 * r
+        t_dadd = adds * (n - 2 * r) ** 2 / rate
+        grid2 = {"value": round(world * fl_g / per_g / 1e9, 3), "unit": "GFLOP/s", "steps": g_steps,
+                 "ms_per_step": round(per_g * 1e3, 4),
+                 "norm_check": abs(nrm_g - 2.0 * (g_steps + args.warmup)) <= 1e-8,
+                 "workload": f"PRK grid stencil R={r}, n={n}, FP64, one fused application per step",
+                 "roofline": {"bound": "binary64 adds" if t_dadd > t_hbm else "hbm",
+                              "hbm": {"achieved": round(bg / per_g / 1e9, 2), "peak": hbm_peak()[0], "unit": "GB/s",
+                                      "frac": round(t_hbm / per_g, 4)},
+                              "binary64_adds": {"adds_per_point": adds, "peak_adds_per_s": round(rate, 1),
+                                                "achieved_adds_per_s": round(adds * (n - 2 * r) ** 2 / per_g, 1),
+                                                "frac": round(t_dadd / per_g, 4),
+                                                "peak_source": "prk_gb300_probe_dadd, measured in this run"},
+                              "note": "the weights are not powers of two, so every product and partial sum "
+                                      "is rounded in the reference's order: one binary64 add per tap"}}
+
+    # ---- the reference's own CUDA stencil (Cxx11/stencil-cuda.cu, sm_103a) beside ours ----
+    comparator = None
+    if not args.no_comparator and rank == 0:
+        comparator = reference_cuda_rate(torch, kg, n, r)
+
     # ---- batched: the seeded 256-grid configuration in one persistent kernel per launch ----
     batched = None
     if not args.no_batch:
@@ -368,7 +438,9 @@ def run_gb300(args) -> None:
     b32 = algorithmic_bytes(n, r, False)
     ach64 = b64 * args.steps / t64 / 1e9
     ach32 = b32 * args.steps / t32 / 1e9
-    traffic = profiled_traffic().get("fp64_star2_n16384_bytes_per_launch")
+    prof = profiled_traffic()
+    traffic = prof.get("fp64_star2_n16384_bytes_per_launch")
+    traffic_src = ("profiles/traffic.json: " + prof.get("source", "")) if traffic else None
     value = world * fl * args.steps / t64 / 1e9
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "GFLOP/s", "n_gpus": world, "steps": args.steps,
@@ -383,7 +455,7 @@ def run_gb300(args) -> None:
         "norm_check": norm_ok,
         "roofline": {"bound": "hbm", "achieved": round(ach64, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(ach64 / peak, 4), "peak_source": peak_kind,
-                     "traffic": traffic, "algorithmic_bytes_per_launch": b64},
+                     "traffic": traffic, "traffic_source": traffic_src, "algorithmic_bytes_per_launch": b64},
         "fp32c": {"value": round(world * fl * args.steps / t32 / 1e9, 3), "unit": "GFLOP/s",
                   "ms_per_step": round(1e3 * t32 / args.steps, 4), "hbm_gbs": round(ach32, 2),
                   "roofline_frac": round(ach32 / peak, 4), "rel_err_vs_fp64": rel32,
@@ -394,6 +466,8 @@ def run_gb300(args) -> None:
                                                 "held in shared memory (temporal blocking); keys are depths, the "
                                                 "largest a whole run of that many applications in one launch",
                      **temporal} if not args.no_temporal else None,
+        "grid2": grid2,
+        "gpu_comparator": comparator,
         "batched": batched,
         "clocks": clocks.summary(),
         "gpu_launches": args.steps,
@@ -423,11 +497,13 @@ def main() -> None:
     ap.add_argument("--radius", type=int, default=R_DEFAULT)
     ap.add_argument("--e2e-iterations", type=int, default=100)
     ap.add_argument("--e2e-steps", type=int, default=5)
-    ap.add_argument("--cpu-applications", type=int, default=3)
+    ap.add_argument("--cpu-applications", type=int, default=100)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-temporal", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-grid", action="store_true")
+    ap.add_argument("--no-comparator", action="store_true")
     ap.add_argument("--batch-iterations", type=int, default=50)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)  # at least 3 untimed warm-up steps

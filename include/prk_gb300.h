@@ -122,6 +122,33 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
 int prk_gb300_run_host(int pattern, int radius, int64_t n, int dtype, int iterations, const void* h_in, void* h_out,
                        void* h_in_final, double* norm, double* elapsed_s, double* kernel_s);
 
+/* ---- One grid split across ranks in row slabs ---------------------------------------------
+ * The reference splits a grid into blocks, one per MPI rank, exchanges an R-wide halo with the
+ * neighbouring ranks before every application, applies the stencil to its block and adds one to its
+ * in, then sums the ranks' norms (MPI1/Stencil/stencil.c:199-268 block split, :338-404 exchange,
+ * :406-420 stencil and in += 1, :425-436 reductions). Here a rank owns the grid rows [row_begin,
+ * row_end) (whole rows, so every halo is contiguous rows of the neighbours' slabs) and its buffers
+ * hold its slab with the halo: grid rows [halo_begin, halo_end) with halo_begin = max(0,
+ * row_begin - R) and halo_end = min(n, row_end + R), row stride n, element layout as for whole
+ * grids. kernels_gb300.decomp does the split, the exchange and the reductions.
+ *
+ * prk_gb300_slab_run: `apps` (>= 1) fused applications in one launch. in holds the current in on
+ * every row of the buffers (the halo rows as the neighbours sent them); in evolves pointwise, so an
+ * R-row halo serves any number of applications. The call adds each application's stencil into out
+ * on the slab's interior points (in the generator's order, as prk_gb300_stencil; FP64 bit-identical
+ * to the whole grid's result) and writes in + apps into in_next on the rows [row_begin, row_end);
+ * in_next's halo rows are not written (the next exchange fills them). Buffers 16-byte aligned with
+ * n a multiple of 2 (FP64) or 4 (FP32C) take the TMA tiles, others the plain-staged tiles.
+ * Stream-ordered. */
+int prk_gb300_slab_run(int pattern, int radius, int64_t n, int dtype, int apps, int64_t row_begin, int64_t row_end,
+                       const void* in, void* in_next, void* out, void* stream);
+
+/* The sum of |out| over the slab's interior points (not divided by (n-2R)^2: the ranks' sums are
+ * added first, as MPI1/Stencil/stencil.c:425-436 reduces them). out is a slab buffer as above.
+ * Synchronous. */
+int prk_gb300_slab_norm(int radius, int64_t n, int dtype, int64_t row_begin, int64_t row_end, const void* out,
+                        double* l1_sum, void* stream);
+
 /* Capacity of the fixed scratch behind prk_gb300_norm_noalloc: partial sums, 8 KiB per device. */
 #define PRK_NOALLOC_NORM_PARTIALS 1024
 
@@ -136,7 +163,9 @@ int prk_gb300_run_host(int pattern, int radius, int64_t n, int dtype, int iterat
  * - norm_dev is caller-owned DEVICE memory for one double; the result is the same value
  *   prk_gb300_norm returns. Stream-ordered and asynchronous: read *norm_dev after the stream.
  * - The first call on each device looks up the scratch's device address (cudaGetSymbolAddress)
- *   with that device current; make that first call before any stream capture.
+ *   with that device current, and keeps it for the CUDA context it belongs to; the first call in a
+ *   new context on that device (e.g. after cudaDeviceReset) looks it up again. Make those first
+ *   calls before any stream capture.
  * - Every call shares the scratch, which keeps the last call's contents (nothing in it needs to
  *   start at zero). Calls that overlap on the GPU, e.g. on two streams, race on it. */
 int prk_gb300_norm_noalloc(int radius, int64_t n, int dtype, const void* out, double* norm_dev, void* stream);
@@ -228,6 +257,12 @@ int prk_gb300_batch_destroy(prk_gb300_batch* batch);
  * barrier nobody arrives on, a short poll limit) and returns what prk_gb300_status reports then:
  * PRK_ERR_TIMEOUT when the timeout path works. The GPU stays usable; nothing faults or hangs. */
 int prk_gb300_selftest_timeout(void);
+
+/* Measures the current device's binary64 add throughput (adds per second) with a short kernel of
+ * independent add chains on every SM. The strict-order FP64 stencils (weights that are not powers of
+ * two) need one rounded binary64 add per tap, so this rate is their second ceiling beside HBM; the
+ * benchmark reports both. Synchronous. No counterpart in the reference. */
+int prk_gb300_probe_dadd(double* adds_per_second);
 
 /* Frees the device buffers and streams prk_gb300_run_host keeps on the current device. */
 int prk_gb300_release(void);

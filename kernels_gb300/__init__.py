@@ -32,7 +32,7 @@ FP64, FP32C = 0, 1
 RUN_GRAPH, RUN_UNFUSED, RUN_TUNED, RUN_TALL, RUN_WHOLE = 1, 2, 4, 8, 16
 
 __all__ = ["STAR", "GRID", "FP64", "FP32C", "PrkError", "apply", "add", "init", "norm", "run", "run_host",
-           "alloc", "apply_steps", "flops", "tune", "Batch", "pattern_of", "dtype_of", "version", "set_kernel", "status", "KERNEL_AUTO",
+           "alloc", "apply_steps", "flops", "probe_dadd", "slab_run", "slab_norm", "tune", "Batch", "pattern_of", "dtype_of", "version", "set_kernel", "status", "KERNEL_AUTO",
            "KERNEL_GENERIC", "KERNEL_TMA"] + \
           [f"{p}{r}" for p in ("star", "grid") for r in range(1, 6)]
 
@@ -91,6 +91,14 @@ def status() -> None:
 
 def version() -> str:
     return load().prk_gb300_version().decode()
+
+
+def probe_dadd() -> float:
+    """The current device's binary64 add throughput in adds per second (prk_gb300_probe_dadd): the
+    ceiling of the strict-order FP64 stencils, which need one rounded add per tap."""
+    res = C.c_double()
+    check(load().prk_gb300_probe_dadd(C.byref(res)))
+    return res.value
 
 
 def flops(pattern: int, radius: int, n: int) -> float:
@@ -189,6 +197,33 @@ def run_host(pattern: int, radius: int, iterations: int, h_in, h_out, h_in_final
                                     None if h_in_final is None else ptr(h_in_final), C.byref(nrm), C.byref(el),
                                     C.byref(ks)))
     return {"norm": nrm.value, "elapsed_s": el.value, "kernel_s": ks.value}
+
+
+def slab_run(pattern: int, radius: int, n: int, apps: int, row_begin: int, row_end: int, in_, in_next, out,
+             stream=None) -> None:
+    """`apps` fused applications on a row slab of an n x n grid (prk_gb300_slab_run): the tensors
+    hold grid rows [max(0, row_begin - R), min(n, row_end + R)) with n columns (FP32C out: [.., n, 2]);
+    out gains each application's stencil on the slab's interior points, in_next = in + apps on the
+    rows [row_begin, row_end)."""
+    dt = dtype_of(in_)
+    lo, hi = max(0, row_begin - radius), min(n, row_end + radius)
+    want = (hi - lo, n)
+    for t in (in_, in_next):
+        if tuple(t.shape) != want or dtype_of(t) != dt or not t.is_contiguous():
+            raise PrkError(-1, f"slab in buffers must be contiguous {want} tensors of one dtype")
+    if tuple(out.shape[:2]) != want or not out.is_contiguous():
+        raise PrkError(-1, f"slab out must be a contiguous tensor of {want} points")
+    check(load().prk_gb300_slab_run(pattern, radius, n, dt, apps, row_begin, row_end, in_.data_ptr(),
+                                    in_next.data_ptr(), out.data_ptr(), _stream(stream)))
+
+
+def slab_norm(radius: int, n: int, row_begin: int, row_end: int, out, stream=None) -> float:
+    """Sum of |out| over a slab's interior points (prk_gb300_slab_norm), not yet divided by (n-2R)^2."""
+    import torch
+    dt = FP64 if out.dtype == torch.float64 else FP32C
+    res = C.c_double()
+    check(load().prk_gb300_slab_norm(radius, n, dt, row_begin, row_end, out.data_ptr(), C.byref(res), _stream(stream)))
+    return res.value
 
 
 def nstream(A, B, C_, scalar: float = 3.0, stream=None) -> None:

@@ -28,6 +28,8 @@ SIGNATURES: dict[str, tuple] = {
     "prk_gb300_add": (_int, [_i64, _int, _vp, _vp]),
     "prk_gb300_init": (_int, [_i64, _int, _vp, _vp, _vp]),
     "prk_gb300_norm": (_int, [_int, _i64, _int, _vp, _pd, _vp]),
+    "prk_gb300_slab_run": (_int, [_int, _int, _i64, _int, _int, _i64, _i64, _vp, _vp, _vp, _vp]),
+    "prk_gb300_slab_norm": (_int, [_int, _i64, _int, _i64, _i64, _vp, _pd, _vp]),
     "prk_gb300_norm_noalloc": (_int, [_int, _i64, _int, _vp, _vp, _vp]),
     "prk_gb300_run": (_int, [_int, _int, _i64, _int, _int, _vp, _vp, _vp, _int, _pd, _pi, _vp]),
     "prk_gb300_run_host": (_int, [_int, _int, _i64, _int, _int, _vp, _vp, _vp, _pd, _pd, _pd]),
@@ -41,6 +43,7 @@ SIGNATURES: dict[str, tuple] = {
     "prk_gb300_batch_norms": (_int, [_vp, _vp, _vp]),
     "prk_gb300_batch_launches": (_int, [_vp, _int]),
     "prk_gb300_batch_destroy": (_int, [_vp]),
+    "prk_gb300_probe_dadd": (_int, [_pd]),
     "prk_gb300_release": (_int, []),
     "prk_gb300_nstream": (_int, [_i64, _dbl, _vp, _vp, _vp, _vp]),
     "prk_gb300_transpose": (_int, [_i64, _vp, _vp, _vp]),

@@ -82,14 +82,24 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     return LIB
 
 
-def build_oracle() -> None:
-    """Compile the CPU oracle (oracle/Makefile), and oracle/_ref when the reference sources exist."""
+def build_oracle(reference: str | None = None) -> None:
+    """Compile the CPU oracle (oracle/Makefile). With a ParRes/Kernels checkout (`reference`, else
+    $PRK_REFERENCE) also compile oracle/_ref, the reference's own drivers, dump harness and CUDA
+    stencil, from the sources where they lie. Without one, say that those are skipped."""
     _run(["make", "-s", "-C", str(ROOT / "oracle"), "all"])
-    ref = Path(os.environ.get("PRK_REFERENCE", "/root/reference"))
+    ref_dir = reference or os.environ.get("PRK_REFERENCE")
+    if not ref_dir:
+        print("no reference checkout given (PRK_REFERENCE unset): oracle/_ref, the reference's own builds, skipped")
+        return
+    ref = Path(ref_dir)
     if (ref / "Cxx11" / "stencil_seq.hpp").exists():
         _run(["make", "-s", "-C", str(ROOT / "oracle"), "ref", f"REF={ref}"])
+    else:
+        print(f"{ref}/Cxx11/stencil_seq.hpp not found: the reference drivers and dump harness skipped")
     if (ref / "Cxx11" / "stencil-cuda.cu").exists():
         _run(["make", "-s", "-C", str(ROOT / "oracle"), "ref-cuda", f"REF={ref}"])
+    else:
+        print(f"{ref}/Cxx11/stencil-cuda.cu not found: the reference CUDA stencil skipped")
 
 
 if __name__ == "__main__":

@@ -48,11 +48,12 @@ struct Layout {
 };
 
 // Stage the `in` tile at (i0, j0) with its halo in shared memory: coalesced plain loads, zero
-// outside the grid, all loads issued before the first shared-memory store. Thread t takes elements
+// outside the arrays (nr rows of n columns), all loads issued before the first shared-memory store. Thread t takes elements
 // t, t + THREADS, ... of the row-major tile; its row, column and grid offset advance by constants
 // from one element to the next (one division per thread, none per element).
 template <int R, int DT>
-__device__ __forceinline__ void stage_tile(unsigned char* smem, const void* in_v, int64_t n, int64_t i0, int64_t j0)
+__device__ __forceinline__ void stage_tile(unsigned char* smem, const void* in_v, int64_t n, int64_t nr, int64_t i0,
+                                           int64_t j0)
 {
     using G = tile::Geo<DT, R>;
     using T = typename tile::Cfg<DT>::T;
@@ -60,7 +61,7 @@ __device__ __forceinline__ void stage_tile(unsigned char* smem, const void* in_v
     constexpr int DR = tile::THREADS / G::SW, DC = tile::THREADS % G::SW;
     const T* __restrict__ in = static_cast<const T*>(in_v);
     T* s_in = reinterpret_cast<T*>(smem);
-    const uint32_t un = static_cast<uint32_t>(n);  // n <= NMAX < 2^31
+    const uint32_t un = static_cast<uint32_t>(n), unr = static_cast<uint32_t>(nr);  // n, nr <= NMAX < 2^31
     int r = threadIdx.x / G::SW, c = threadIdx.x - (threadIdx.x / G::SW) * G::SW;
     int gi = static_cast<int>(i0) - R + r, gj = static_cast<int>(j0) - G::RA + c;
     int64_t off = static_cast<int64_t>(gi) * n + gj;
@@ -69,7 +70,7 @@ __device__ __forceinline__ void stage_tile(unsigned char* smem, const void* in_v
     for (int q = 0; q < PER; ++q) {  // all loads first, then the shared-memory stores
         const int idx = threadIdx.x + q * tile::THREADS;
         const bool ok = (q + 1) * tile::THREADS <= G::ELEMS || idx < G::ELEMS;
-        v[q] = (ok && static_cast<uint32_t>(gi) < un && static_cast<uint32_t>(gj) < un) ? in[off] : T(0);
+        v[q] = (ok && static_cast<uint32_t>(gi) < unr && static_cast<uint32_t>(gj) < un) ? in[off] : T(0);
         c += DC;
         gi += DR;
         gj += DC;
@@ -98,9 +99,9 @@ __device__ __forceinline__ void item(unsigned char* smem, int* s_red, const Grid
     const int64_t n = g.n;
     const int64_t i0 = (t / g.tiles_x) * C::TH;
     const int64_t j0 = (t % g.tiles_x) * C::TW;
-    stage_tile<R, DT>(smem, g.in[parity], n, i0, j0);
+    stage_tile<R, DT>(smem, g.in[parity], n, n, i0, j0);
     tile::process_tile<P, R, DT, STEPS, tile::OUT_HBM>(smem, s_red, i0, j0, n, tile::tile_has_out(i0, j0, n, R, C::TW, C::TH),
-                                               g.in[parity ^ 1], g.out, g.vec_ok != 0, depth);
+                                               g.in[parity ^ 1], g.out, g.vec_ok != 0, depth, 0, n);
 }
 
 template <int DT, int STEPS>

@@ -66,10 +66,12 @@ bool overlaps(const void* a, int64_t abytes, const void* b, int64_t bbytes)
 
 // Library-owned device scratch: NORM_BLOCKS partial sums and the result for the norm, and the
 // status word the tile kernels set when a bounded wait gives up. One allocation per device, kept
-// until the process exits.
+// until the process exits, with the id of the context it was made in: in a new context on the device
+// (after cudaDeviceReset, which freed it) it is allocated again.
 struct DevScratch {
     double* norm = nullptr;
     unsigned* status = nullptr;
+    unsigned long long context = 0;
 };
 std::mutex g_scratch_mu;
 std::vector<DevScratch> g_scratch;
@@ -80,6 +82,9 @@ int dev_scratch(DevScratch* out)
     PRK_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
     std::lock_guard<std::mutex> lock(g_scratch_mu);
     if (static_cast<int>(g_scratch.size()) <= dev) g_scratch.resize(dev + 1);
+    const unsigned long long ctx = prk::current_context_id();
+    if (g_scratch[dev].norm && ctx != 0 && g_scratch[dev].context != 0 && ctx != g_scratch[dev].context)
+        g_scratch[dev] = DevScratch{};  // the old context and its memory are gone
     if (!g_scratch[dev].norm) {
         void* p = nullptr;
         const size_t bytes = (prk::NORM_BLOCKS + 1) * sizeof(double) + 256;
@@ -92,6 +97,7 @@ int dev_scratch(DevScratch* out)
         if (e != cudaSuccess) return cuda_fail(e, "cudaMemset of the library scratch");
         g_scratch[dev].norm = static_cast<double*>(p);
         g_scratch[dev].status = reinterpret_cast<unsigned*>(static_cast<char*>(p) + (prk::NORM_BLOCKS + 1) * sizeof(double));
+        g_scratch[dev].context = prk::current_context_id();
     }
     *out = g_scratch[dev];
     return PRK_OK;
@@ -112,6 +118,7 @@ struct HostWorkspace {
     void* d[3] = {nullptr, nullptr, nullptr};
     int64_t in_bytes = 0, out_bytes = 0;
     cudaStream_t s[4] = {nullptr, nullptr, nullptr, nullptr};
+    unsigned long long context = 0;  // the context the buffers and streams belong to
 };
 std::mutex g_host_mu;
 std::vector<HostWorkspace> g_host_ws;
@@ -204,6 +211,38 @@ int prk_gb300_selftest_timeout(void)
     PRK_CUDA(prk::launch_wait_selftest(d.status, nullptr), "self-test launch");
     PRK_CUDA(cudaDeviceSynchronize(), "self-test");
     return check_status();
+}
+
+int prk_gb300_probe_dadd(double* adds_per_second)
+{
+    if (!adds_per_second) return fail(PRK_ERR_ARG, "adds_per_second must be non-null");
+    DevScratch d;
+    if (int rc = dev_scratch(&d)) return rc;
+    int dev = 0, sms = 0;
+    PRK_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    PRK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+    const int blocks = sms * 8, iters = 4096;
+    cudaStream_t s = nullptr;
+    PRK_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = PRK_OK;
+    do {
+        cudaError_t ce;
+        if ((ce = cudaEventCreate(&e0)) != cudaSuccess || (ce = cudaEventCreate(&e1)) != cudaSuccess) { rc = cuda_fail(ce, "cudaEventCreate"); break; }
+        if ((ce = prk::launch_dadd_probe(d.norm, blocks, iters / 16, 0.5, s)) != cudaSuccess) { rc = cuda_fail(ce, "probe launch"); break; }
+        cudaEventRecord(e0, s);
+        if ((ce = prk::launch_dadd_probe(d.norm, blocks, iters, 0.5, s)) != cudaSuccess) { rc = cuda_fail(ce, "probe launch"); break; }
+        cudaEventRecord(e1, s);
+        if ((ce = cudaEventSynchronize(e1)) != cudaSuccess) { rc = cuda_fail(ce, "probe"); break; }
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        *adds_per_second = static_cast<double>(blocks) * 256.0 * 8.0 * (iters + 1) / (ms * 1e-3);
+    } while (false);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    return rc;
 }
 
 int64_t prk_gb300_bytes(int64_t n, int dtype, int role)
@@ -422,6 +461,62 @@ int prk_gb300_run(int pattern, int radius, int64_t n, int dtype, int iterations,
     return rc;
 }
 
+int prk_gb300_slab_run(int pattern, int radius, int64_t n, int dtype, int apps, int64_t row_begin, int64_t row_end,
+                       const void* in, void* in_next, void* out, void* stream)
+{
+    if (int rc = check_stencil(pattern, radius, n, dtype)) return rc;
+    if (apps < 1) return fail(PRK_ERR_ARG, "apps must be >= 1");
+    if (row_begin < 0 || row_end > n || row_begin >= row_end)
+        return fail(PRK_ERR_ARG, "slab rows [%lld, %lld) are empty or outside the grid of %lld rows",
+                    static_cast<long long>(row_begin), static_cast<long long>(row_end), static_cast<long long>(n));
+    if (!in || !in_next || !out) return fail(PRK_ERR_ARG, "in, in_next and out must be non-null device pointers");
+    const int64_t halo_begin = std::max<int64_t>(0, row_begin - radius);
+    const int64_t halo_end = std::min<int64_t>(n, row_end + radius);
+    const int64_t nr = halo_end - halo_begin;
+    const int64_t ib = nr * n * prk::in_elem_bytes(dtype), ob = nr * n * prk::out_elem_bytes(dtype);
+    if (overlaps(in, ib, out, ob) || overlaps(in_next, ib, in, ib) || overlaps(in_next, ib, out, ob))
+        return fail(PRK_ERR_ARG, "buffers overlap");
+    if (g_kernel_choice == 1) return fail(PRK_ERR_ARG, "slab runs need the tile kernels");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    prk::StencilCall c{pattern, radius, n, dtype, in, in_next, out, s, nr, halo_begin};
+    const int64_t row0 = row_begin - halo_begin, rows = row_end - row_begin;
+    if (prk::tma_eligible(c)) {
+        DevScratch d;
+        if (int rc = dev_scratch(&d)) return rc;
+        if (prk::tma_depth_ok(apps))
+            PRK_CUDA(prk::launch_stencil_tma_rows(c, apps, row0, rows, d.status), "slab launch (TMA tiles)");
+        else
+            PRK_CUDA(prk::launch_stencil_tma_band(c, apps, row0, rows, d.status), "slab launch (TMA tiles)");
+        return PRK_OK;
+    }
+    if (g_kernel_choice == 2 || !prk::plain_eligible(c))
+        return fail(PRK_ERR_ARG, "slab buffers must be aligned to their element size%s",
+                    g_kernel_choice == 2 ? ", 16-byte-aligned with n a multiple of the vector width for TMA" : "");
+    PRK_CUDA(prk::launch_stencil_plain(c, apps, row0, rows), "slab launch (plain-staged tiles)");
+    return PRK_OK;
+}
+
+int prk_gb300_slab_norm(int radius, int64_t n, int dtype, int64_t row_begin, int64_t row_end, const void* out,
+                        double* l1_sum, void* stream)
+{
+    if (int rc = check_common(radius, n, dtype)) return rc;
+    if (row_begin < 0 || row_end > n || row_begin >= row_end)
+        return fail(PRK_ERR_ARG, "slab rows [%lld, %lld) are empty or outside the grid of %lld rows",
+                    static_cast<long long>(row_begin), static_cast<long long>(row_end), static_cast<long long>(n));
+    if (!out || !l1_sum) return fail(PRK_ERR_ARG, "out and l1_sum must be non-null");
+    double* scratch = nullptr;
+    if (int rc = norm_scratch(&scratch)) return rc;
+    const int64_t halo_begin = std::max<int64_t>(0, row_begin - radius);
+    const int64_t lo = std::max<int64_t>(row_begin, radius) - halo_begin;
+    const int64_t hi = std::min<int64_t>(row_end, n - radius) - halo_begin;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    PRK_CUDA(prk::launch_norm_rows(radius, n, dtype, out, lo, hi, 1.0, scratch, scratch + prk::NORM_BLOCKS, s),
+             "slab norm launch");
+    PRK_CUDA(cudaMemcpyAsync(l1_sum, scratch + prk::NORM_BLOCKS, sizeof(double), cudaMemcpyDeviceToHost, s), "norm copy");
+    PRK_CUDA(cudaStreamSynchronize(s), "norm synchronize");
+    return PRK_OK;
+}
+
 }  // extern "C"
 
 namespace {
@@ -537,6 +632,10 @@ int prk_gb300_run_host(int pattern, int radius, int64_t n, int dtype, int iterat
     std::lock_guard<std::mutex> lock(g_host_mu);  // one host-buffer run per process at a time
     if (static_cast<int>(g_host_ws.size()) <= dev) g_host_ws.resize(dev + 1);
     HostWorkspace& ws = g_host_ws[dev];
+    {
+        const unsigned long long ctx = prk::current_context_id();
+        if (ws.context != 0 && ctx != 0 && ctx != ws.context) ws = HostWorkspace{};  // freed with the old context
+    }
     int rc = PRK_OK;
     do {
         cudaError_t ce;
@@ -559,6 +658,7 @@ int prk_gb300_run_host(int pattern, int radius, int64_t n, int dtype, int iterat
             }
             ws.in_bytes = ib;
             ws.out_bytes = ob;
+            ws.context = prk::current_context_id();
         }
         void** d = ws.d;
         {

@@ -146,34 +146,107 @@ __device__ __forceinline__ double block_sum(double v)
 
 constexpr int NORM_THREADS = 256;
 
-// Per-block partial sums of |out| over interior rows blockIdx.x, blockIdx.x + gridDim.x, ...
-// FP64: binary64 accumulation. FP32C: each |hi+lo| is accumulated as a two-float sum per thread and
-// widened to binary64 once at the end.
+// |d| as an unevaluated pair of floats h + l, from the binary64 encoding alone (the binary64 pipe
+// runs conversions at its slow rate): h holds the top 24 bits of the significand and l the next 23,
+// rounded on the bit below, so |(h + l) - |d|| <= 2^-47 |d|. Returns false, leaving h and l
+// untouched, when d is zero or its exponent lies outside [2^-60, 2^77), where the pair's exponents
+// would leave float's normal range; the caller adds such values in binary64.
+__device__ __forceinline__ bool abs_as_float_pair(uint64_t b, float& h, float& l)
+{
+    const uint32_t hi = static_cast<uint32_t>(b >> 32) & 0x7FFFFFFFu, lo = static_cast<uint32_t>(b);
+    const uint32_t e = hi >> 20;  // biased binary64 exponent
+    if (e < 963u || e >= 1100u) return false;
+    // h: same exponent (rebias by 1023 - 127 = 896), fraction bits 51..29
+    h = __uint_as_float(((e - 896u) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29));
+    // l: fraction bits 28..6, rounded half up on bit 5, as an integer x <= 2^23 worth
+    // x * 2^(e - 1075 + 6): float(x) by the 2^23 magic number (exact; x = 2^23 carries into the
+    // exponent field and still comes out exact), then scaled by that power of two (exact, normal for
+    // e >= 963)
+    const uint32_t xi = (((lo >> 5) & 0xFFFFFFu) + 1u) >> 1;
+    const float x = __fsub_rn(__uint_as_float(0x4B000000u | xi), 8388608.0f);
+    l = __fmul_rn(x, __uint_as_float((e - 1075u + 6u + 127u) << 23));
+    return true;
+}
+
+// Per-block partial sums of |out| over the interior columns of array rows i_lo + blockIdx.x,
+// i_lo + blockIdx.x + gridDim.x, ... below i_hi.
+// Both forms accumulate per thread as a two-float sum (TwoSum on the high parts, the errors and the
+// low parts into the low word) and widen to binary64 once per thread at the end: FP32C from its
+// (hi, lo) words, FP64 from each |value| split into a float pair by abs_as_float_pair (relative
+// error at most 2^-47 per value; values outside that range, zeros aside, go into a binary64 sum).
+// Four columns per thread per trip keep four loads in flight. The order of every sum is fixed, so
+// the result is deterministic.
 template <int DT>
-__global__ void __launch_bounds__(NORM_THREADS) k_norm_partial(int R, int64_t n, const void* out_v, double* partial)
+__global__ void __launch_bounds__(NORM_THREADS) k_norm_partial(int R, int64_t n, int64_t i_lo, int64_t i_hi,
+                                                               const void* out_v, double* partial)
 {
     double acc = 0.0;
     float ah = 0.0f, al = 0.0f;
-    for (int64_t i = R + blockIdx.x; i < n - R; i += gridDim.x) {
-        for (int64_t j = R + threadIdx.x; j < n - R; j += NORM_THREADS) {
+    auto add_pair = [&](float h, float l) {
+        float t, e;
+        two_sum(ah, h, t, e);
+        ah = t;
+        al = __fadd_rn(al, __fadd_rn(e, l));
+    };
+    constexpr int U = 4;
+    for (int64_t i = i_lo + blockIdx.x; i < i_hi; i += gridDim.x) {
+        const int64_t end = n - R;
+        for (int64_t j0 = R + threadIdx.x; j0 < end; j0 += U * NORM_THREADS) {
             if constexpr (DT == FP64) {
-                acc = __dadd_rn(acc, fabs(static_cast<const double*>(out_v)[i * n + j]));
-            } else {
-                float2 o = static_cast<const float2*>(out_v)[i * n + j];
-                if (o.x < 0.0f || (o.x == 0.0f && o.y < 0.0f)) {
-                    o.x = -o.x;
-                    o.y = -o.y;
+                const uint64_t* row = static_cast<const uint64_t*>(out_v) + i * n;
+                uint64_t b[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int64_t j = j0 + u * NORM_THREADS;
+                    b[u] = j < end ? row[j] : 0ull;
                 }
-                float t, e;
-                two_sum(ah, o.x, t, e);
-                ah = t;
-                al = __fadd_rn(al, __fadd_rn(e, o.y));
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    float h, l;
+                    if (abs_as_float_pair(b[u], h, l))
+                        add_pair(h, l);
+                    else if ((b[u] << 1) != 0ull)
+                        acc = __dadd_rn(acc, fabs(__longlong_as_double(static_cast<long long>(b[u]))));
+                }
+            } else {
+                const float2* row = static_cast<const float2*>(out_v) + i * n;
+                float2 o[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int64_t j = j0 + u * NORM_THREADS;
+                    o[u] = j < end ? row[j] : make_float2(0.0f, 0.0f);
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    if (o[u].x < 0.0f || (o[u].x == 0.0f && o[u].y < 0.0f)) {
+                        o[u].x = -o[u].x;
+                        o[u].y = -o[u].y;
+                    }
+                    add_pair(o[u].x, o[u].y);
+                }
             }
         }
     }
-    if constexpr (DT != FP64) acc = static_cast<double>(ah) + static_cast<double>(al);
+    acc = __dadd_rn(acc, __dadd_rn(static_cast<double>(ah), static_cast<double>(al)));
     const double tot = block_sum<NORM_THREADS>(acc);
     if (threadIdx.x == 0) partial[blockIdx.x] = tot;
+}
+
+// Binary64 add throughput: every thread runs 8 independent chains of `iters` adds. The sum is
+// stored only when it equals a value the chains cannot reach, which keeps the adds live.
+__global__ void __launch_bounds__(256) k_dadd_probe(double* sink, double step, int iters)
+{
+    double a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = static_cast<double>(threadIdx.x) + 0.125 * k;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = __dadd_rn(a[k], step);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s = __dadd_rn(s, a[k]);
+    if (s == -1.0) sink[0] = s;
 }
 
 // Sum of the partials in a fixed order, scaled by 1/(n-2R)^2.
@@ -226,19 +299,33 @@ cudaError_t launch_init(int64_t n, int dtype, void* in, void* out, cudaStream_t 
     return cudaGetLastError();
 }
 
+cudaError_t launch_dadd_probe(double* sink, int blocks, int iters, double step, cudaStream_t s)
+{
+    k_dadd_probe<<<blocks, 256, 0, s>>>(sink, step, iters);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_norm_rows(int R, int64_t n, int dtype, const void* out, int64_t i_lo, int64_t i_hi, double divisor,
+                             double* partial, double* result_dev, cudaStream_t s)
+{
+    const int64_t rows = i_hi > i_lo ? i_hi - i_lo : 0;
+    const int blocks = static_cast<int>(rows < NORM_BLOCKS ? rows : NORM_BLOCKS);
+    if (blocks > 0) {
+        if (dtype == FP64)
+            k_norm_partial<FP64><<<blocks, NORM_THREADS, 0, s>>>(R, n, i_lo, i_hi, out, partial);
+        else
+            k_norm_partial<FP32C><<<blocks, NORM_THREADS, 0, s>>>(R, n, i_lo, i_hi, out, partial);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    k_norm_final<<<1, NORM_THREADS, 0, s>>>(partial, blocks, divisor, result_dev);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_norm(int R, int64_t n, int dtype, const void* out, double* partial, double* result_dev, cudaStream_t s)
 {
-    const int64_t rows = n - 2 * R;
-    const int blocks = static_cast<int>(rows < NORM_BLOCKS ? rows : NORM_BLOCKS);
-    if (dtype == FP64)
-        k_norm_partial<FP64><<<blocks, NORM_THREADS, 0, s>>>(R, n, out, partial);
-    else
-        k_norm_partial<FP32C><<<blocks, NORM_THREADS, 0, s>>>(R, n, out, partial);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    const double active = static_cast<double>(rows) * static_cast<double>(rows);
-    k_norm_final<<<1, NORM_THREADS, 0, s>>>(partial, blocks, active, result_dev);
-    return cudaGetLastError();
+    const double active = static_cast<double>(n - 2 * R) * static_cast<double>(n - 2 * R);
+    return launch_norm_rows(R, n, dtype, out, R, n - R, active, partial, result_dev, s);
 }
 
 }  // namespace prk

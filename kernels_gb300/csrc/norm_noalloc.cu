@@ -11,16 +11,48 @@
 // The scratch is the file-scope array below. Host code must not pass the array's name to a kernel:
 // on the host that name denotes a host-side shadow, not device memory. A kernel handed it would
 // fault, or, on a system where the GPU can reach host memory, silently read and write the wrong
-// memory. The device address is obtained once per device with cudaGetSymbolAddress, with that device
-// current, on the first call made on that device; that first call should therefore come before any
-// stream capture. Every call shares the array: it is not cleared between calls (the norm kernels
-// write every partial they later read, so nothing needs to start at zero), and calls that overlap on
-// the GPU (for instance on two streams) race on it and give undefined results.
+// memory. The device address is looked up with cudaGetSymbolAddress, with the device current, on
+// the first call made on that device, and kept together with the identity of the CUDA context it
+// belongs to (cuCtxGetId). A later call in another context on that device (after cudaDeviceReset,
+// which loads the library's module again, possibly at another address) looks it up again. The first
+// call on a device, and the first after a reset, should therefore come before any stream capture.
+// Every call shares the array: it is not cleared between calls (the norm kernels write every partial
+// they later read, so nothing needs to start at zero), and calls that overlap on the GPU (for
+// instance on two streams) race on it and give undefined results.
+#include <cudaTypedefs.h>
+
 #include <cstdio>
 #include <mutex>
 
 #include "../../include/prk_gb300.h"
 #include "prk_internal.cuh"
+
+namespace prk {
+
+// Unique id of the calling thread's current CUDA context, 0 when there is none or the driver gives
+// none. The driver entry points come through the runtime, so the library does not link libcuda.
+unsigned long long current_context_id()
+{
+    static std::once_flag once;
+    static PFN_cuCtxGetCurrent_v4000 get_current = nullptr;
+    static PFN_cuCtxGetId_v12000 get_id = nullptr;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(p);
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(p);
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+}  // namespace prk
 
 namespace {
 
@@ -32,11 +64,16 @@ static __device__ __align__(256) double g_norm_scratch[NOALLOC_SCRATCH_DOUBLES];
 
 constexpr int MAX_DEVICES = 64;
 std::mutex g_mu;
-double* g_scratch_dev[MAX_DEVICES] = {};
+struct ScratchAddress {
+    double* ptr = nullptr;
+    unsigned long long context = 0;  // cuCtxGetId of the context the address belongs to
+};
+ScratchAddress g_scratch_dev[MAX_DEVICES];
 
 int fail(int code, const char* msg) { return prk::record_error(code, msg); }
 
-// Device address of the scratch on the current device, looked up once per device.
+// Device address of the scratch in the current device's current context: looked up once per device
+// and context.
 int scratch_address(double** out)
 {
     int dev = 0;
@@ -44,17 +81,20 @@ int scratch_address(double** out)
     if (e != cudaSuccess) return fail(static_cast<int>(e), "prk_gb300_norm_noalloc: cudaGetDevice failed");
     if (dev < 0 || dev >= MAX_DEVICES) return fail(PRK_ERR_LIMIT, "prk_gb300_norm_noalloc: device ordinal above 63");
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_dev[dev]) {
+    ScratchAddress& a = g_scratch_dev[dev];
+    const unsigned long long ctx = prk::current_context_id();
+    if (!a.ptr || ctx == 0 || ctx != a.context) {
         void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_norm_scratch);
+        e = cudaGetSymbolAddress(&p, g_norm_scratch);  // also makes the device's primary context current
         if (e != cudaSuccess) {
             char msg[256];
             std::snprintf(msg, sizeof msg, "prk_gb300_norm_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
             return fail(static_cast<int>(e), msg);
         }
-        g_scratch_dev[dev] = static_cast<double*>(p);
+        a.ptr = static_cast<double*>(p);
+        a.context = prk::current_context_id();
     }
-    *out = g_scratch_dev[dev];
+    *out = a.ptr;
     return PRK_OK;
 }
 

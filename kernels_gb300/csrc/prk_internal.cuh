@@ -8,7 +8,9 @@
 
 namespace prk {
 
-// One stencil application as the C ABI describes it (prk_gb300_stencil).
+// One stencil application as the C ABI describes it (prk_gb300_stencil). The buffers hold the whole
+// n x n grid, or (nr > 0) a row slab of it: nr rows from grid row goff, row stride n
+// (prk_gb300_slab_run).
 struct StencilCall {
     int pattern;
     int R;
@@ -18,6 +20,8 @@ struct StencilCall {
     void* in_next;  // may be null: stencil only, in untouched
     void* out;
     cudaStream_t stream;
+    int64_t nr = 0;    // rows the buffers hold (0: n)
+    int64_t goff = 0;  // grid row of the buffers' row 0
 };
 
 // Largest n the tile grids address (gridDim.y = ceil(n/16) <= 65535).
@@ -37,16 +41,18 @@ bool tma_depth_ok(int steps);
 // Tile heights the TMA kernels are built for (32 and 64 rows).
 bool tma_rows_ok(int tile_rows);
 cudaError_t launch_stencil_tma(const StencilCall& c, int steps, unsigned* status, int tile_rows = 32);
-// All `depth` applications of a run in one launch over the tiles of grid rows [row0, row0 + rows)
-// (row0 a multiple of 32): reads `in` rows row0 - R .. row0 + rows + R - 1 and the band's `out`
-// rows, writes the band's in_next (in after `depth` updates) and out rows.
+// All `depth` applications of a run in one launch over the tiles of buffer rows [row0, row0 + rows):
+// reads `in` rows row0 - R .. row0 + rows + R - 1 (those the buffers hold; zero beyond) and the
+// band's `out` rows, writes the band's in_next (in after `depth` updates) and out rows.
 cudaError_t launch_stencil_tma_band(const StencilCall& c, int depth, int64_t row0, int64_t rows, unsigned* status);
+// The same over buffer rows [row0, row0 + rows) with the compile-time depth `steps` (1, 2, 4 or 8).
+cudaError_t launch_stencil_tma_rows(const StencilCall& c, int steps, int64_t row0, int64_t rows, unsigned* status);
 
 // tile_plain_*.cu: the fused form on shapes the TMA kernels cannot take (any n, buffers aligned to
 // their element size); the tile staged with plain loads, then evaluated as in the TMA kernels.
-// `depth` applications in one launch (1 for one application per launch), over the tiles of grid
-// rows [row0, row0 + rows) (row0 a multiple of 32; rows = 0: to the last row), reading `in` rows
-// row0 - R .. row0 + rows + R - 1 as launch_stencil_tma_band does.
+// `depth` applications in one launch (1 for one application per launch), over the tiles of buffer
+// rows [row0, row0 + rows) (rows = 0: to the last row), reading `in` rows row0 - R .. row0 + rows +
+// R - 1 as launch_stencil_tma_band does.
 bool plain_eligible(const StencilCall& c);
 cudaError_t launch_stencil_plain(const StencilCall& c, int depth, int64_t row0 = 0, int64_t rows = 0);
 
@@ -58,6 +64,18 @@ cudaError_t launch_init(int64_t n, int dtype, void* in, void* out, cudaStream_t 
 constexpr int NORM_BLOCKS = 1024;
 cudaError_t launch_norm(int R, int64_t n, int dtype, const void* out, double* partial, double* result_dev,
                         cudaStream_t s);
+// The sum of |out| over the interior columns R..n-R-1 of array rows [i_lo, i_hi) (row stride n),
+// divided by `divisor`, to *result_dev; the same kernels and fixed order as launch_norm.
+cudaError_t launch_norm_rows(int R, int64_t n, int dtype, const void* out, int64_t i_lo, int64_t i_hi, double divisor,
+                             double* partial, double* result_dev, cudaStream_t s);
+
+// Binary64 add throughput probe: `blocks` CTAs of 256 threads, 8 chains of `iters` adds each.
+cudaError_t launch_dadd_probe(double* sink, int blocks, int iters, double step, cudaStream_t s);
+
+// Unique id of the calling thread's current CUDA context (cuCtxGetId), 0 when there is none or the
+// driver gives none (norm_noalloc.cu). Device addresses the library caches are kept with the id of
+// the context they belong to: after cudaDeviceReset the device's context, and its memory, are new.
+unsigned long long current_context_id();
 
 // Records `msg` as the calling thread's prk_gb300_last_error() and returns `code` (capi.cu).
 int record_error(int code, const char* msg);

@@ -97,8 +97,10 @@ struct Launch {
     unsigned* status;
     cudaStream_t stream;
     int depth;     // applications per launch for the run-time-depth kernels (STEPS = 0)
-    int64_t row0;  // first grid row of the launch's tiles (a multiple of the tile height)
-    int64_t rows;  // grid rows covered from row0 (0: to the end of the grid)
+    int64_t row0;  // first array row of the launch's tiles
+    int64_t rows;  // array rows covered from row0 (0: to the last row of the arrays)
+    int64_t nr;    // rows the arrays hold (0: n, a whole grid); the tensor maps cover nr x n
+    int64_t goff;  // grid row of the arrays' row 0
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -712,10 +714,13 @@ constexpr int OUT_SMEM = 0, OUT_HBM = 1, OUT_HBM_AHEAD = 2;
 // STEPS = 0), then in_next and out to HBM, with out read from OUT_SRC. vec_ok: rows are 16-byte
 // aligned and n is a multiple of CPT, so a thread's CPT points move as one vector; otherwise they
 // move one by one.
+// The arrays hold rows of an n x n grid (row stride n); i0 is the tile's first row in the arrays and
+// goff the grid row of the arrays' row 0 (0 for a whole grid; a row slab's first row otherwise).
+// Rows from row_end on (in the arrays) are not stored; the interior test uses grid rows.
 template <int P, int R, int DT, int STEPS, int OUT_SRC = OUT_SMEM, int TH_ = 32>
 __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, int64_t i0, int64_t j0, int64_t n,
                                              bool has_out, void* __restrict__ in_next_v, void* __restrict__ out_v,
-                                             bool vec_ok = true, int depth = 0)
+                                             bool vec_ok, int depth, int64_t goff, int64_t row_end)
 {
     const int nsteps = STEPS > 0 ? STEPS : depth;
     using G = Geo<DT, R, TH_>;
@@ -998,8 +1003,8 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
 #pragma unroll
             for (int rr = 0; rr < ROWS; ++rr) {
                 const int r = warp * ROWS + rr;
-                const int64_t gi = i0 + r;
-                const bool row_out = col_ok && gi < n && has_out && gi >= R && gi < n - R;
+                const int64_t gi = i0 + r, gg = gi + goff;
+                const bool row_out = col_ok && gi < row_end && has_out && gg >= R && gg < n - R;
 #pragma unroll
                 for (int k = 0; k < CPT; ++k) o_pre[rr][k] = row_out ? load_out(r, k) : 0ull;
             }
@@ -1007,9 +1012,9 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
 #pragma unroll
         for (int rr = 0; rr < ROWS; ++rr) {
             const int r = warp * ROWS + rr;
-            const int64_t gi = i0 + r;
-            if (!col_ok || gi >= n) continue;
-            const bool row_out = has_out && gi >= R && gi < n - R;
+            const int64_t gi = i0 + r, gg = gi + goff;
+            if (!col_ok || gi >= row_end) continue;
+            const bool row_out = has_out && gg >= R && gg < n - R;
             uint64_t o[CPT];
             if (row_out) {
 #pragma unroll
@@ -1031,8 +1036,8 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
 #pragma unroll
         for (int rr = 0; rr < ROWS; ++rr) {
             const int r = warp * ROWS + rr;
-            const int64_t gi = i0 + r;
-            ract[rr] = col_ok && gi < n && has_out && gi >= R && gi < n - R;
+            const int64_t gi = i0 + r, gg = gi + goff;
+            ract[rr] = col_ok && gi < row_end && has_out && gg >= R && gg < n - R;
 #pragma unroll
             for (int k = 0; k < CPT; ++k) o[rr][k] = ract[rr] ? load_out(r, k) : 0ull;
         }
@@ -1170,9 +1175,9 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
 #pragma unroll
         for (int rr = 0; rr < ROWS; ++rr) {
             const int r = warp * ROWS + rr;
-            const int64_t gi = i0 + r;
-            if (!col_ok || gi >= n) continue;
-            store_row(r, o[rr], has_out && gi >= R && gi < n - R);
+            const int64_t gi = i0 + r, gg = gi + goff;
+            if (!col_ok || gi >= row_end) continue;
+            store_row(r, o[rr], has_out && gg >= R && gg < n - R);
         }
     }
 }
@@ -1194,12 +1199,14 @@ constexpr int min_blocks()
 
 // One CTA per tile: blockIdx = (tile column, tile row). The elected thread issues the tile's two TMA
 // loads; every thread waits on the mbarrier with a bounded spin, and on a timeout the CTA flags
-// `status`, waits (again bounded) for the copies to land and returns.
+// `status`, waits (again bounded) for the copies to land and returns. The arrays hold rows of the
+// n x n grid from grid row goff (the tensor maps cover exactly the rows they hold, so the hardware
+// zero-fills anything beyond); rows from row_end on are read as halo but not stored.
 template <int P, int R, int DT, int STEPS, int TH_>
 __global__ void __launch_bounds__(THREADS, min_blocks<P, R, DT, STEPS, TH_>())
     k_stencil_tile(const __grid_constant__ CUtensorMap tm_in, const __grid_constant__ CUtensorMap tm_out,
                    const int64_t n, void* __restrict__ in_next_v, void* __restrict__ out_v, unsigned* __restrict__ status,
-                   const int depth, const int64_t row0)
+                   const int depth, const int64_t row0, const int64_t goff, const int64_t row_end)
 {
     using G = Geo<DT, R, TH_>;
     using C = Cfg<DT, TH_>;
@@ -1208,7 +1215,7 @@ __global__ void __launch_bounds__(THREADS, min_blocks<P, R, DT, STEPS, TH_>())
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + G::BAR_OFF);
     const int64_t i0 = row0 + static_cast<int64_t>(blockIdx.y) * C::TH;
     const int64_t j0 = static_cast<int64_t>(blockIdx.x) * C::TW;
-    const bool has_out = tile_has_out(i0, j0, n, R, C::TW, C::TH);
+    const bool has_out = tile_has_out(i0 + goff, j0, n, R, C::TW, C::TH);
 
     if (threadIdx.x == 0) {
         mbar_init(bar, 1);
@@ -1218,12 +1225,15 @@ __global__ void __launch_bounds__(THREADS, min_blocks<P, R, DT, STEPS, TH_>())
         if (has_out) tma_load_2d(smem + G::OUT_OFF, &tm_out, static_cast<int32_t>(j0), static_cast<int32_t>(i0), bar);
     }
     __syncthreads();
-    if (!mbar_wait_bounded(bar, 0)) {
+    // One decision for the whole CTA: process_tile's barriers need every thread, so the tile is
+    // evaluated only when every thread saw the loads land.
+    if (!__syncthreads_and(mbar_wait_bounded(bar, 0))) {
         if (threadIdx.x == 0) atomicOr(status, 1u);
         mbar_wait_bounded(bar, 0);  // let the copies land before the CTA's shared memory is released
         return;
     }
-    process_tile<P, R, DT, STEPS, OUT_SMEM, TH_>(smem, s_red, i0, j0, n, has_out, in_next_v, out_v, true, depth);
+    process_tile<P, R, DT, STEPS, OUT_SMEM, TH_>(smem, s_red, i0, j0, n, has_out, in_next_v, out_v, true, depth, goff,
+                                                 row_end);
 }
 
 template <int P, int R, int DT, int STEPS, int TH_>
@@ -1233,14 +1243,16 @@ cudaError_t launch(const Launch& L)
     using C = Cfg<DT, TH_>;
     if (cudaError_t e = cudaFuncSetAttribute(k_stencil_tile<P, R, DT, STEPS, TH_>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM))
         return e;
-    if (L.row0 < 0 || L.row0 % C::TH != 0 || L.row0 >= L.n || L.rows < 0 || (STEPS == 0 && L.depth < 1))
+    const int64_t nr = L.nr > 0 ? L.nr : L.n;
+    if (L.row0 < 0 || L.row0 >= nr || L.rows < 0 || (STEPS == 0 && L.depth < 1) || L.goff < 0 || L.goff + nr > L.n)
         return cudaErrorInvalidValue;
-    const int64_t rows = L.rows > 0 && L.rows < L.n - L.row0 ? L.rows : L.n - L.row0;
+    const int64_t rows = L.rows > 0 && L.rows < nr - L.row0 ? L.rows : nr - L.row0;
     const int64_t tx = (L.n + C::TW - 1) / C::TW, ty = (rows + C::TH - 1) / C::TH;
     if (ty > 65535) return cudaErrorInvalidValue;
     const dim3 grid(static_cast<unsigned>(tx), static_cast<unsigned>(ty));
     k_stencil_tile<P, R, DT, STEPS, TH_><<<grid, THREADS, G::SMEM, L.stream>>>(L.tm_in, L.tm_out, L.n, L.in_next, L.out,
-                                                                             L.status, L.depth, L.row0);
+                                                                             L.status, L.depth, L.row0, L.goff,
+                                                                             L.row0 + rows);
     return cudaGetLastError();
 }
 

@@ -28,12 +28,12 @@ cudaError_t encoder(PFN_cuTensorMapEncodeTiled_v12000* fn)
     return g_encode_err;
 }
 
-// A 2D map over an n x n row-major array of elem_bytes elements, box (box_x, box_y), zero fill.
-cudaError_t make_map(CUtensorMap* map, const void* base, int64_t n, int elem_bytes, int box_x, int box_y)
+// A 2D map over a row-major array of nr rows of n elem_bytes elements, box (box_x, box_y), zero fill.
+cudaError_t make_map(CUtensorMap* map, const void* base, int64_t n, int64_t nr, int elem_bytes, int box_x, int box_y)
 {
     PFN_cuTensorMapEncodeTiled_v12000 enc = nullptr;
     if (cudaError_t e = encoder(&enc)) return e;
-    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(n), static_cast<cuuint64_t>(n)};
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(n), static_cast<cuuint64_t>(nr)};
     const cuuint64_t strides[1] = {static_cast<cuuint64_t>(n) * elem_bytes};
     const cuuint32_t box[2] = {static_cast<cuuint32_t>(box_x), static_cast<cuuint32_t>(box_y)};
     const cuuint32_t estr[2] = {1, 1};
@@ -106,14 +106,20 @@ bool plain_eligible(const StencilCall& c)
 cudaError_t launch_stencil_plain(const StencilCall& c, int depth, int64_t row0, int64_t rows)
 {
     if (depth < 1 || !plain_eligible(c)) return cudaErrorInvalidValue;
-    const plain::Args a{c.in, c.in_next, c.out, c.n, depth, c.stream, row0, rows};
+    const plain::Args a{c.in, c.in_next, c.out, c.n, depth, c.stream, row0, rows, c.nr, c.goff};
     return c.dtype == FP64 ? plain::launch_fp64(c.pattern, c.R, a) : plain::launch_fp32c(c.pattern, c.R, a);
 }
 
 cudaError_t launch_stencil_tma_band(const StencilCall& c, int depth, int64_t row0, int64_t rows, unsigned* status)
 {
-    if (depth < 1 || row0 < 0 || row0 % tile::TH_DEFAULT != 0 || rows < 1) return cudaErrorInvalidValue;
+    if (depth < 1 || row0 < 0 || rows < 1) return cudaErrorInvalidValue;
     return launch_tma(c, 0, status, tile::TH_DEFAULT, depth, row0, rows);
+}
+
+cudaError_t launch_stencil_tma_rows(const StencilCall& c, int steps, int64_t row0, int64_t rows, unsigned* status)
+{
+    if (!tma_depth_ok(steps) || row0 < 0 || rows < 1) return cudaErrorInvalidValue;
+    return launch_tma(c, steps, status, tile::TH_DEFAULT, 0, row0, rows);
 }
 
 namespace {
@@ -124,8 +130,11 @@ cudaError_t launch_tma(const StencilCall& c, int steps, unsigned* status, int ti
     tile::Launch L{};
     int ix, iy, ox, oy;
     tile::boxes(c.dtype, c.R, tile_rows, &ix, &iy, &ox, &oy);
-    if (cudaError_t e = make_map(&L.tm_in, c.in, c.n, c.dtype == FP64 ? 8 : 4, ix, iy)) return e;
-    if (cudaError_t e = make_map(&L.tm_out, c.out, c.n, 8, ox, oy)) return e;
+    const int64_t nr = c.nr > 0 ? c.nr : c.n;
+    if (cudaError_t e = make_map(&L.tm_in, c.in, c.n, nr, c.dtype == FP64 ? 8 : 4, ix, iy)) return e;
+    if (cudaError_t e = make_map(&L.tm_out, c.out, c.n, nr, 8, ox, oy)) return e;
+    L.nr = nr;
+    L.goff = c.goff;
     L.n = c.n;
     L.in_next = c.in_next;
     L.out = c.out;

@@ -34,25 +34,27 @@ constexpr int plain_min_blocks()
 }
 
 // blockIdx = (tile column, tile row counted from row0). The evaluation is compiled for one-by-one
-// stores only (the shapes here never allow the 16-byte vectors).
+// stores only (the shapes here never allow the 16-byte vectors). The arrays hold nr rows of the
+// n x n grid from grid row goff; rows from row_end on are read as halo but not stored.
 template <int P, int R, int DT, int STEPS>
 __global__ void __launch_bounds__(tile::THREADS, plain_min_blocks<P, R, DT, STEPS>())
     k_stencil_plain(const void* __restrict__ in, void* __restrict__ in_next, void* __restrict__ out, const int64_t n,
-                    const int depth, const int64_t row0)
+                    const int depth, const int64_t row0, const int64_t nr, const int64_t goff, const int64_t row_end)
 {
     using C = tile::Cfg<DT>;
     extern __shared__ __align__(128) unsigned char smem[];
     int* s_red = reinterpret_cast<int*>(smem + Smem<DT, R>::RED_OFF);
     const int64_t i0 = row0 + static_cast<int64_t>(blockIdx.y) * C::TH;
     const int64_t j0 = static_cast<int64_t>(blockIdx.x) * C::TW;
-    const bool has_out = tile::tile_has_out(i0, j0, n, R, C::TW, C::TH);
-    batch::stage_tile<R, DT>(smem, in, n, i0, j0);
-    tile::process_tile<P, R, DT, STEPS, tile::OUT_HBM_AHEAD>(smem, s_red, i0, j0, n, has_out, in_next, out, false, depth);
+    const bool has_out = tile::tile_has_out(i0 + goff, j0, n, R, C::TW, C::TH);
+    batch::stage_tile<R, DT>(smem, in, n, nr, i0, j0);
+    tile::process_tile<P, R, DT, STEPS, tile::OUT_HBM_AHEAD>(smem, s_red, i0, j0, n, has_out, in_next, out, false, depth,
+                                                             goff, row_end);
 }
 
 // The arguments of one launch: `depth` applications from in into in_next, accumulating into out,
-// over the tiles of grid rows [row0, row0 + rows) (row0 a multiple of the tile height; rows = 0:
-// to the last row).
+// over the tiles of array rows [row0, row0 + rows) (rows = 0: to the last row). The arrays hold
+// nr rows (0: n) of the n x n grid, from grid row goff.
 struct Args {
     const void* in;
     void* in_next;
@@ -62,6 +64,8 @@ struct Args {
     cudaStream_t stream;
     int64_t row0;
     int64_t rows;
+    int64_t nr;
+    int64_t goff;
 };
 
 template <int P, int R, int DT, int STEPS>
@@ -71,12 +75,15 @@ cudaError_t launch(const Args& a)
     constexpr int SM = Smem<DT, R>::BYTES;
     if (cudaError_t e = cudaFuncSetAttribute(k_stencil_plain<P, R, DT, STEPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM))
         return e;
-    if (a.row0 < 0 || a.row0 % C::TH != 0 || a.row0 >= a.n || a.rows < 0 || a.depth < 1) return cudaErrorInvalidValue;
-    const int64_t rows = a.rows > 0 && a.rows < a.n - a.row0 ? a.rows : a.n - a.row0;
+    const int64_t nr = a.nr > 0 ? a.nr : a.n;
+    if (a.row0 < 0 || a.row0 >= nr || a.rows < 0 || a.depth < 1 || a.goff < 0 || a.goff + nr > a.n)
+        return cudaErrorInvalidValue;
+    const int64_t rows = a.rows > 0 && a.rows < nr - a.row0 ? a.rows : nr - a.row0;
     const int64_t tx = (a.n + C::TW - 1) / C::TW, ty = (rows + C::TH - 1) / C::TH;
     if (ty > 65535) return cudaErrorInvalidValue;
     const dim3 grid(static_cast<unsigned>(tx), static_cast<unsigned>(ty));
-    k_stencil_plain<P, R, DT, STEPS><<<grid, tile::THREADS, SM, a.stream>>>(a.in, a.in_next, a.out, a.n, a.depth, a.row0);
+    k_stencil_plain<P, R, DT, STEPS><<<grid, tile::THREADS, SM, a.stream>>>(a.in, a.in_next, a.out, a.n, a.depth, a.row0,
+                                                                          nr, a.goff, a.row0 + rows);
     return cudaGetLastError();
 }
 

@@ -317,6 +317,37 @@ double prk_oracle_norm(int R, int64_t n, const double* out)
     return norm / ((double)(n - 2 * R) * (double)(n - 2 * R));
 }
 
+/* One application out += S(in) on a row slab of an n x n grid: in and out hold the grid rows
+ * [first, first + nrows) with row stride n, and the points updated are the interior points of the
+ * grid rows [row_begin, row_end) (which must lie inside the held rows, with R more either side
+ * wherever the grid has them). Each point in the generator's strict order, as prk_oracle_apply: the
+ * ranks of MPI1/Stencil/stencil.c:406-420 apply the stencil to their own block the same way.
+ * Returns 0, or -1 on bad arguments. */
+int prk_oracle_apply_rows(int pattern, int R, int64_t n, int64_t first, int64_t nrows, int64_t row_begin,
+                          int64_t row_end, const double* in, double* out)
+{
+    if (check_args(pattern, R, n)) return -1;
+    if (first < 0 || nrows < 1 || first + nrows > n || row_begin < first || row_end > first + nrows || row_begin > row_end)
+        return -1;
+    const int64_t lo = row_begin > R ? row_begin : R, hi = row_end < n - R ? row_end : n - R;
+    if (lo < hi && (lo - R < first || hi + R > first + nrows)) return -1; /* the halo must be held */
+    int dc[128], dr[128];
+    double w[128];
+    const int taps = prk_oracle_taps(pattern, R, dc, dr, w);
+    for (int64_t i = lo; i < hi; ++i) {
+        const double* row = in + (i - first) * n;
+        for (int64_t j = R; j < n - R; ++j) {
+            double s = 0.0;
+            for (int q = 0; q < taps; ++q) {
+                const double p = row[dr[q] * n + j + dc[q]] * w[q];
+                s = (q == 0) ? p : s + p;
+            }
+            out[(i - first) * n + j] = out[(i - first) * n + j] + s;
+        }
+    }
+    return 0;
+}
+
 /* out(i,j) after `applications` applications of a PRK run, computed for one interior point
  * without a grid: in_k(i,j) = i+j+k is exact in binary64 below 2^53, so the reference's value is
  * the left-to-right evaluation of the generated expression on those integers. Works for any n. */

@@ -37,6 +37,8 @@ def _load(name: str) -> C.CDLL:
     lib.prk_oracle_taps.argtypes = [i, i, vp, vp, vp]
     lib.prk_oracle_apply.restype = i
     lib.prk_oracle_apply.argtypes = [i, i, i64, i64, vp, vp]
+    lib.prk_oracle_apply_rows.restype = i
+    lib.prk_oracle_apply_rows.argtypes = [i, i, i64, i64, i64, i64, i64, vp, vp]
     lib.prk_oracle_add.restype = i
     lib.prk_oracle_add.argtypes = [i64, i64, vp]
     lib.prk_oracle_init.restype = i
@@ -91,6 +93,18 @@ def apply(pattern: int, radius: int, in_: np.ndarray, out: np.ndarray, tile: int
     n = in_.shape[0]
     if oracle().prk_oracle_apply(pattern, radius, n, tile, in_.ctypes.data, out.ctypes.data) != 0:
         raise ValueError("oracle rejected the arguments")
+
+
+def apply_rows(pattern: int, radius: int, n: int, first: int, row_begin: int, row_end: int, in_: np.ndarray,
+               out: np.ndarray) -> None:
+    """One strict-order application on a row slab (in place): in_ and out hold grid rows
+    [first, first + in_.shape[0]) of an n x n grid; the interior points of rows [row_begin, row_end)
+    are updated."""
+    assert in_.dtype == np.float64 and out.dtype == np.float64 and in_.flags.c_contiguous and out.flags.c_contiguous
+    assert in_.shape == out.shape and in_.shape[1] == n
+    if oracle().prk_oracle_apply_rows(pattern, radius, n, first, in_.shape[0], row_begin, row_end, in_.ctypes.data,
+                                      out.ctypes.data) != 0:
+        raise ValueError("oracle rejected the slab arguments")
 
 
 def norm(radius: int, out: np.ndarray) -> float:
