@@ -120,3 +120,31 @@ def test_neighbour_rejections(cuda):
     assert lib.prk_gb300_transpose(32, M.data_ptr(), M.data_ptr(), None) == -1  # A is B
     assert lib.prk_gb300_transpose(0, M.data_ptr(), M.data_ptr(), None) == -1
     assert lib.prk_gb300_transpose(1 << 23, M.data_ptr(), None, None) == -1
+
+
+def _sha(a) -> str:
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<f8").tobytes()).hexdigest()
+
+
+def test_gpu_reproduces_reference_driver_arrays(cuda):
+    """The arrays the reference's own nstream and transpose drivers (Cxx11/nstream.cc,
+    Cxx11/transpose.cc) left after their runs (tests/golden/neighbours_golden.json), bit for bit."""
+    import json
+    from pathlib import Path
+    g = json.loads((Path(__file__).resolve().parent / "golden" / "neighbours_golden.json").read_text())
+    for c in g["nstream"]:
+        n = c["length"]
+        A = cuda.zeros(n, dtype=cuda.float64, device="cuda")
+        B = cuda.full((n,), 2.0, dtype=cuda.float64, device="cuda")
+        C = cuda.full((n,), 2.0, dtype=cuda.float64, device="cuda")
+        for _ in range(c["iterations"] + 1):
+            kg.nstream(A, B, C, scalar=3.0)
+        assert (_sha(A.cpu().numpy()), _sha(B.cpu().numpy()), _sha(C.cpu().numpy())) == \
+            (c["A_sha256"], c["B_sha256"], c["C_sha256"]), c
+    for c in g["transpose"]:
+        a, b = nb.transpose_init(c["order"])
+        A, B = cuda.from_numpy(a).cuda(), cuda.from_numpy(b).cuda()
+        for _ in range(c["iterations"] + 1):
+            kg.transpose(A, B)
+        assert (_sha(A.cpu().numpy()), _sha(B.cpu().numpy())) == (c["A_sha256"], c["B_sha256"]), c
