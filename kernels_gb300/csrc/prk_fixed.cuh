@@ -160,6 +160,113 @@ PRK_HD uint64_t mul_whole20(uint64_t wb, int32_t v)
     return mul_whole20_split(static_cast<uint32_t>(wb), (whi & 0xFFFFFu) | 0x100000u, whi & 0xFFF00000u, v);
 }
 
+// ---- 96-bit fixed point for the strict-order sums ------------------------------------------------
+// The stencils whose weights are not powers of two round every product and every partial sum of the
+// reference's chain (((p1 + p2) + p3) + ...). On tiles of whole numbers |v| < 2^20 every product
+// p = fl(w * v) of a PRK weight (|w| >= 1/900) is a multiple of 2^-62 (its lowest bit lies at most 52
+// places below its leading bit, which is at or above 2^-10), and every partial sum, being the rounded
+// sum of such multiples, is one too; all stay below 2^22 in magnitude (sum |w| <= 2). Each value is
+// then an integer of units 2^-62 below 2^84, held exactly in three 32-bit words as a two's-complement
+// number, and a rounded binary64 add is: the exact integer sum, then rounding to 53 significant bits
+// at the position its leading bit sets, to nearest with ties to the even neighbour. Both steps are
+// integer instructions, so a chain can leave the binary64 pipe for the integer pipes and come back
+// with the same bits (fx96_to_bits).
+constexpr int FX96_F = 62;
+
+// x = v * 2^62 for a binary64 v (encoding b) with |v| < 2^22 that is a multiple of 2^-62, or +-0.
+PRK_HD void fx96_from_bits(uint64_t b, uint32_t& x0, uint32_t& x1, uint32_t& x2)
+{
+    x0 = x1 = x2 = 0;
+    if ((b << 1) == 0) return;
+    const int e = static_cast<int>((b >> 52) & 0x7FF);
+    const uint64_t m = (b & MANT) | HIDDEN;  // v = m * 2^(e - 1075)
+    const int sh = e - 1075 + FX96_F;       // v * 2^62 = m * 2^sh, sh <= 31 for |v| < 2^22
+    uint64_t lo;
+    uint32_t hi;
+    if (sh >= 0) {
+        lo = m << sh;
+        hi = sh == 0 ? 0u : static_cast<uint32_t>(m >> (64 - sh));
+    } else {
+        lo = m >> (-sh);  // the bits shifted out are zero for a multiple of 2^-62
+        hi = 0u;
+    }
+    if (b & SIGN) {  // two's-complement negation of the 96-bit value
+        lo = ~lo + 1;
+        hi = ~hi + (lo == 0 ? 1u : 0u);
+    }
+    x0 = static_cast<uint32_t>(lo);
+    x1 = static_cast<uint32_t>(lo >> 32);
+    x2 = hi;
+}
+
+// x = fl(x + p) (SUB: fl(x - p)) for 96-bit fixed-point values whose exact result lies below 2^84
+// units: the exact sum, then rounding to 53 significant bits, nearest-even. The position b of the
+// rounding is the leading bit of |sum| less 52, at most 31, so only the low word is cut and the
+// rounding increment carries into the others. Rounding the two's-complement value to a multiple of
+// 2^b with ties to the even multiple gives the same result as rounding its magnitude and negating;
+// the leading bit is read from the one's complement of a negative sum, which differs from the
+// magnitude's only when the magnitude is a power of two (then nothing lies below b anyway).
+template <bool SUB>
+PRK_HD void fx96_acc_round(uint32_t& x0, uint32_t& x1, uint32_t& x2, uint32_t p0, uint32_t p1, uint32_t p2)
+{
+#ifdef __CUDA_ARCH__
+    if (SUB)
+        asm("sub.cc.u32 %0, %0, %3;\n\tsubc.cc.u32 %1, %1, %4;\n\tsubc.u32 %2, %2, %5;"
+            : "+r"(x0), "+r"(x1), "+r"(x2)
+            : "r"(p0), "r"(p1), "r"(p2));
+    else
+        asm("add.cc.u32 %0, %0, %3;\n\taddc.cc.u32 %1, %1, %4;\n\taddc.u32 %2, %2, %5;"
+            : "+r"(x0), "+r"(x1), "+r"(x2)
+            : "r"(p0), "r"(p1), "r"(p2));
+#else
+    const uint64_t a = (static_cast<uint64_t>(x1) << 32) | x0, pq = (static_cast<uint64_t>(p1) << 32) | p0;
+    const uint64_t r = SUB ? a - pq : a + pq;
+    const uint32_t c = SUB ? (a < pq ? 1u : 0u) : (r < a ? 1u : 0u);
+    x2 = SUB ? x2 - p2 - c : x2 + p2 + c;
+    x0 = static_cast<uint32_t>(r);
+    x1 = static_cast<uint32_t>(r >> 32);
+#endif
+    const uint32_t sg = static_cast<uint32_t>(static_cast<int32_t>(x2) >> 31);
+    const uint32_t t2 = x2 ^ sg, t1 = x1 ^ sg;
+    int b = t2 ? 43 - clz32(t2) : 11 - clz32(t1);
+    b = b < 0 ? 0 : b;
+    const uint32_t mask = (1u << b) - 1u;
+    const uint32_t q = (x0 >> b) & (mask & 1u);  // lowest kept bit; 0 when nothing is cut
+    const uint32_t inc = (((x0 & mask) + (mask >> 1) + q) >> b) << b;
+    const uint32_t cut = x0 & ~mask;
+#ifdef __CUDA_ARCH__
+    asm("add.cc.u32 %0, %3, %4;\n\taddc.cc.u32 %1, %1, 0;\n\taddc.u32 %2, %2, 0;"
+        : "=r"(x0), "+r"(x1), "+r"(x2)
+        : "r"(cut), "r"(inc));
+#else
+    const uint64_t old = (static_cast<uint64_t>(x1) << 32) | cut, lo = old + inc;
+    x2 += lo < old ? 1u : 0u;
+    x0 = static_cast<uint32_t>(lo);
+    x1 = static_cast<uint32_t>(lo >> 32);
+#endif
+}
+
+// The binary64 encoding of x * 2^-62 for a value with at most 53 significant bits (a rounded sum)
+// and |x| < 2^84. Zero gives +0, or -0 when negzero (a chain of -0 terms sums to -0).
+PRK_HD uint64_t fx96_to_bits(uint32_t x0, uint32_t x1, uint32_t x2, bool negzero)
+{
+    const uint32_t sg = static_cast<uint32_t>(static_cast<int32_t>(x2) >> 31);
+    uint64_t lo = ((static_cast<uint64_t>(x1) << 32) | x0) ^ ((static_cast<uint64_t>(sg) << 32) | sg);
+    uint32_t hi = x2 ^ sg;
+    lo += sg & 1u;  // + 1 completes the negation of a negative value
+    hi += (sg & 1u) && lo == 0 ? 1u : 0u;
+    if ((lo | hi) == 0) return negzero ? SIGN : 0ull;
+    const int msb = hi ? 95 - clz32(hi) : 63 - clz64(lo);
+    uint64_t m;  // the significand, leading bit at position 52
+    if (msb >= 52) {
+        const int sa = msb - 52;  // 0 .. 31: the bits below are zero (x is rounded)
+        m = sa == 0 ? lo : ((static_cast<uint64_t>(hi) << (64 - sa)) | (lo >> sa));
+    } else {
+        m = lo << (52 - msb);
+    }
+    return (static_cast<uint64_t>(sg) << 63) | ((static_cast<uint64_t>(msb - FX96_F + 1022) << 52) + m);
+}
+
 // Certification of a tile whose values have lowest-bit exponents >= lo_min and highest-bit
 // exponents <= hi_max, for a stencil with weight shift `shift` and coefficient L1 norm `coef_l1`
 // (sum |w| * 2^shift), and `steps` in += 1 updates applied to the tile before its last use.

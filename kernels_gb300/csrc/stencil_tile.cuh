@@ -696,6 +696,267 @@ __device__ __forceinline__ void advance_i32(int32_t* p)
 }
 
 // ---------------------------------------------------------------------------------------------
+// FP64 stencils whose weights are not powers of two, on whole-number tiles of small range: the
+// table route (TMA tiles only).
+//
+// Every product and every partial sum of the reference's chain rounds, and GB300 issues binary64
+// adds at a small fraction of its integer rate, so the route moves work off the binary64 pipe
+// without changing a bit:
+//  - Products from a table. A tile whose values all lie in [base, base + TBL_L) takes each product
+//    fl(|w| * v) from a shared-memory table of every weight group and every such v, built once per
+//    tile with fx::mul_whole20 (the weight's sign enters as an add or a subtract). Every tap still
+//    reads its own in value, and indexes the table with it.
+//  - The first fixed_taps() adds of each point's chain run in 96-bit fixed point on the integer
+//    pipes (fx::fx96_acc_round: the exact sum rounded to 53 bits, nearest-even, the binary64 add's
+//    result bit for bit on these values), the rest and the add into out on the binary64 pipe.
+// Lane l evaluates columns l and l + 32 of its warp's rows, so a warp's table reads are consecutive
+// entries; the results go into the shared-memory out tile, which the stores then read in their own
+// layout. Applications of a multi-application launch advance the int32 tile in place, as the other
+// routes do, and the table is rebuilt at a new base when the values outgrow it.
+
+constexpr int TBL_L = 128;  // consecutive values one product table covers
+
+// The tables follow the TMA kernel's own shared memory (16-byte aligned).
+template <int DT, int R, int TH_>
+__host__ __device__ constexpr int table_offset()
+{
+    return (Geo<DT, R, TH_>::SMEM + 15) / 16 * 16;
+}
+
+template <int P, int R>
+struct StrictTaps {
+    int dc[tap_count(P, R)], dr[tap_count(P, R)], g[tap_count(P, R)], neg[tap_count(P, R)];
+};
+
+// The taps in the generator's order (column offset outer, row offset inner, zeros left out), each
+// with its weight group and sign.
+template <int P, int R>
+constexpr StrictTaps<P, R> make_strict_taps()
+{
+    StrictTaps<P, R> t{};
+    int k = 0;
+    for (int dc = -R; dc <= R; ++dc)
+        for (int dr = -R; dr <= R; ++dr) {
+            const double w = weight(P, R, dc, dr);
+            if (w != 0.0) {
+                t.dc[k] = dc;
+                t.dr[k] = dr;
+                t.g[k] = group_of<P, R>(dc, dr);
+                t.neg[k] = w < 0.0 ? 1 : 0;
+                ++k;
+            }
+        }
+    return t;
+}
+
+// Every tap's |weight| is its group's (checked for the stencils the route serves).
+template <int P, int R>
+constexpr bool strict_taps_ok()
+{
+    constexpr StrictTaps<P, R> t = make_strict_taps<P, R>();
+    for (int k = 0; k < tap_count(P, R); ++k) {
+        const double w = weight(P, R, t.dc[k], t.dr[k]);
+        if ((w < 0.0 ? -w : w) != group_weight<P, R>(t.g[k])) return false;
+    }
+    return true;
+}
+static_assert(strict_taps_ok<STAR, 3>() && strict_taps_ok<STAR, 4>() && strict_taps_ok<STAR, 5>() &&
+                  strict_taps_ok<GRID, 2>() && strict_taps_ok<GRID, 3>() && strict_taps_ok<GRID, 4>() &&
+                  strict_taps_ok<GRID, 5>(),
+              "strict tap groups");
+
+// Sixteenths of each chain that run in fixed point (the rest stays on the binary64 pipe).
+#ifndef PRK_FX_SIXTEENTHS
+#define PRK_FX_SIXTEENTHS 11
+#endif
+
+template <int P, int R>
+constexpr int fixed_taps()
+{
+    const int k = tap_count(P, R) * PRK_FX_SIXTEENTHS / 16;
+    return k < 1 ? 1 : (k > tap_count(P, R) ? tap_count(P, R) : k);
+}
+
+// True when a positive weight lies among the fixed taps: then the fixed part never sums to -0 (a
+// rounded sum is -0 only when every term is -0, and w * v with w > 0 is never -0).
+template <int P, int R>
+constexpr bool fixed_prefix_has_positive()
+{
+    constexpr StrictTaps<P, R> t = make_strict_taps<P, R>();
+    for (int k = 0; k < fixed_taps<P, R>(); ++k)
+        if (!t.neg[k]) return true;
+    return false;
+}
+
+template <int P, int R, int DT>
+__host__ __device__ constexpr bool table_route()
+{
+    return DT == FP64 && !pow2_weights(P, R);
+}
+
+// Shared memory of the tables: per weight group TBL_L binary64 products and TBL_L fixed-point images.
+template <int P, int R, int DT>
+__host__ __device__ constexpr int table_bytes()
+{
+    return table_route<P, R, DT>() ? group_count<P, R>() * TBL_L * (8 + 16) : 0;
+}
+
+// Dynamic shared memory of the TMA kernel: its tile stages, and the tables where the route applies.
+template <int P, int R, int DT, int TH_>
+__host__ __device__ constexpr int tile_smem()
+{
+    return table_offset<DT, R, TH_>() + table_bytes<P, R, DT>();
+}
+
+// Fill the tables for the values [base, base + TBL_L): T64[g * TBL_L + u] = fl(|w_g| * (base + u))
+// and T96 its fixed-point image. Values at or beyond 2^20 in magnitude (never read) get 0.
+template <int P, int R>
+__device__ __forceinline__ void build_tables(uint64_t* T64, uint4* T96, int base)
+{
+    constexpr int NG = group_count<P, R>();
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+        const uint64_t wb = encode(group_weight<P, R>(g));
+        for (int u = threadIdx.x; u < TBL_L; u += THREADS) {
+            const int v = base + u;
+            const uint64_t p = (v > -(1 << 20) && v < (1 << 20)) ? fx::mul_whole20(wb, v) : 0ull;
+            uint32_t x0, x1, x2;
+            fx::fx96_from_bits(p, x0, x1, x2);
+            T64[g * TBL_L + u] = p;
+            T96[g * TBL_L + u] = make_uint4(x0, x1, x2, 0u);
+        }
+    }
+}
+
+// x = fl(x + s * p) in fixed point, s the tap's sign.
+__device__ __forceinline__ void fx96_tap(uint32_t (&x)[3], const uint4& p, int neg)
+{
+    if (neg)
+        fx::fx96_acc_round<true>(x[0], x[1], x[2], p.x, p.y, p.z);
+    else
+        fx::fx96_acc_round<false>(x[0], x[1], x[2], p.x, p.y, p.z);
+}
+
+// One application to the points (r, c) and (r, c + 32) of the thread's rows: the reference chain of
+// each point, then out += S, into the shared-memory out tile. si points at the int32 tile's (0, 0)
+// (row stride SW), o_tile is the out tile (row stride TW). Only the interior points are written.
+template <int P, int R, int SW, int TW, int ROWS>
+__device__ __forceinline__ void table_application(const int32_t* si, uint64_t* o_tile, const uint64_t* T64,
+                                                  const uint4* T96, int base, int64_t i0, int64_t j0, int64_t n,
+                                                  int64_t goff, int64_t row_end, bool has_out)
+{
+    constexpr StrictTaps<P, R> TP = make_strict_taps<P, R>();
+    constexpr int N = tap_count(P, R), KF = fixed_taps<P, R>();
+    constexpr bool POS = fixed_prefix_has_positive<P, R>();
+    static_assert(TW == 64, "two columns per lane, 32 apart");
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll 1
+    for (int rr = 0; rr < ROWS; ++rr) {
+        const int r = warp * ROWS + rr;
+        const int64_t gi = i0 + r, gg = gi + goff;
+        if (!has_out || gi >= row_end || gg < R || gg >= n - R) continue;  // warp-uniform
+        const int32_t* sp = si + r * SW + lane;
+        uint32_t x[2][3];
+        int anyv[2] = {0, 0};
+#pragma unroll
+        for (int t = 0; t < KF; ++t) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int v = sp[TP.dr[t] * SW + TP.dc[t] + 32 * h];
+                if (!POS) anyv[h] |= v;
+                const uint4 p = T96[TP.g[t] * TBL_L + (v - base)];
+                if (t == 0) {
+                    if (TP.neg[t]) {  // x = -p, the 96-bit two's-complement negation
+                        x[h][0] = ~p.x + 1u;
+                        x[h][1] = ~p.y + (p.x == 0u ? 1u : 0u);
+                        x[h][2] = ~p.z + ((p.x | p.y) == 0u ? 1u : 0u);
+                    } else {
+                        x[h][0] = p.x;
+                        x[h][1] = p.y;
+                        x[h][2] = p.z;
+                    }
+                } else {
+                    fx96_tap(x[h], p, TP.neg[t]);
+                }
+            }
+        }
+        double d[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) d[h] = as_dbl(fx::fx96_to_bits(x[h][0], x[h][1], x[h][2], !POS && anyv[h] == 0));
+#pragma unroll
+        for (int t = KF; t < N; ++t) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int v = sp[TP.dr[t] * SW + TP.dc[t] + 32 * h];
+                const double p = as_dbl(T64[TP.g[t] * TBL_L + (v - base)]);
+                d[h] = TP.neg[t] ? __dsub_rn(d[h], p) : __dadd_rn(d[h], p);
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int c = lane + 32 * h;
+            const int64_t gj = j0 + c;
+            if (gj >= R && gj < n - R) o_tile[r * TW + c] = as_bits(__dadd_rn(as_dbl(o_tile[r * TW + c]), d[h]));
+        }
+    }
+}
+
+// The table route for a whole tile: `nsteps` applications into the out tile, with the int32 tile
+// (holding the tile's in, halo included) advanced in place between them, as the other routes leave
+// it for the stores. Returns false, having done nothing, when the tile's values span TBL_L or more
+// (block-uniform; s_red holds two ints per warp).
+template <int P, int R, int SW, int SH, int TW, int ROWS>
+__device__ __forceinline__ bool table_tile(int32_t* si, uint64_t* o_tile, unsigned char* tbl, int* s_red, int nsteps,
+                                           int64_t i0, int64_t j0, int64_t n, int64_t goff, int64_t row_end,
+                                           bool has_out)
+{
+    constexpr int ELEMS = SW * SH;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int lo = 0x7FFFFFFF, hi = -0x7FFFFFFF;
+    for (int idx = threadIdx.x; idx < ELEMS; idx += THREADS) {
+        lo = min(lo, si[idx]);
+        hi = max(hi, si[idx]);
+    }
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    hi = __reduce_max_sync(0xffffffffu, hi);
+    if (lane == 0) {
+        s_red[2 * warp] = lo;
+        s_red[2 * warp + 1] = hi;
+    }
+    __syncthreads();
+    lo = s_red[0];
+    hi = s_red[1];
+#pragma unroll
+    for (int w = 1; w < WARPS; ++w) {
+        lo = min(lo, s_red[2 * w]);
+        hi = max(hi, s_red[2 * w + 1]);
+    }
+    __syncthreads();  // s_red read by every thread before anyone reuses it
+    if (hi - lo >= TBL_L) return false;
+    uint64_t* T64 = reinterpret_cast<uint64_t*>(tbl);
+    uint4* T96 = reinterpret_cast<uint4*>(tbl + group_count<P, R>() * TBL_L * 8);
+    int base = lo;
+    build_tables<P, R>(T64, T96, base);
+    __syncthreads();
+    const int32_t* s0 = si + R * SW + ((SW - TW) / 2);  // the tile's (0, 0)
+#pragma unroll 1
+    for (int t = 0; t < nsteps; ++t) {
+        if (t > 0) {
+            advance_i32<ELEMS>(si);
+            if (hi + t >= base + TBL_L) {  // the values outgrew the table: rebuild it at the new minimum
+                base = lo + t;
+                build_tables<P, R>(T64, T96, base);
+            }
+            __syncthreads();
+        }
+        table_application<P, R, SW, TW, ROWS>(s0, o_tile, T64, T96, base, i0, j0, n, goff, row_end, has_out);
+        if (t + 1 < nsteps) __syncthreads();  // every thread's reads done before the next advance
+    }
+    __syncthreads();  // the out tile complete before the stores read it in their layout
+    return true;
+}
+
+// ---------------------------------------------------------------------------------------------
 // The kernel
 
 // True when the tile at (i0, j0) holds interior points, i.e. has an out tile to load and update.
@@ -851,6 +1112,15 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
             }
         }
         __syncthreads();
+    }
+
+    // ---- FP64, other weights, TMA tiles: the table route (table_tile), when the range allows ----
+    bool tbl_done = false;
+    if constexpr (table_route<P, R, DT>() && OUT_SRC == OUT_SMEM) {
+        if (iwhole)
+            tbl_done = table_tile<P, R, G::SW, G::SH, C::TW, ROWS>(reinterpret_cast<int32_t*>(s_in), o_tile,
+                                                                   stage + table_offset<DT, R, TH_>(), s_red, nsteps,
+                                                                   i0, j0, n, goff, row_end, has_out);
     }
 
     // Set by the multi-application FP32 route when the tile's out words are held as integers
@@ -1024,7 +1294,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
                     else
                         o[k] = load_out(r, k);
                 }
-                apply_row(r, o);
+                if (!tbl_done) apply_row(r, o);
             }
             store_row(r, o, row_out);
         }
@@ -1116,7 +1386,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
                 }
                 fin_off = ((nsteps - 1) & 1) * G::ELEMS;
             }
-        } else {
+        } else if (!tbl_done) {
 #pragma unroll 1
         for (int t = 0; t < nsteps; ++t) {
             if (t > 0) {  // advance the whole tile, halo included: in_{k+1} = in_k + 1
@@ -1239,9 +1509,10 @@ __global__ void __launch_bounds__(THREADS, min_blocks<P, R, DT, STEPS, TH_>())
 template <int P, int R, int DT, int STEPS, int TH_>
 cudaError_t launch(const Launch& L)
 {
-    using G = Geo<DT, R, TH_>;
     using C = Cfg<DT, TH_>;
-    if (cudaError_t e = cudaFuncSetAttribute(k_stencil_tile<P, R, DT, STEPS, TH_>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM))
+    constexpr int SMEM = tile_smem<P, R, DT, TH_>();
+    static_assert(SMEM <= SMEM_PER_CTA_MAX, "the tile and its tables must fit in shared memory");
+    if (cudaError_t e = cudaFuncSetAttribute(k_stencil_tile<P, R, DT, STEPS, TH_>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM))
         return e;
     const int64_t nr = L.nr > 0 ? L.nr : L.n;
     if (L.row0 < 0 || L.row0 >= nr || L.rows < 0 || (STEPS == 0 && L.depth < 1) || L.goff < 0 || L.goff + nr > L.n)
@@ -1250,7 +1521,7 @@ cudaError_t launch(const Launch& L)
     const int64_t tx = (L.n + C::TW - 1) / C::TW, ty = (rows + C::TH - 1) / C::TH;
     if (ty > 65535) return cudaErrorInvalidValue;
     const dim3 grid(static_cast<unsigned>(tx), static_cast<unsigned>(ty));
-    k_stencil_tile<P, R, DT, STEPS, TH_><<<grid, THREADS, G::SMEM, L.stream>>>(L.tm_in, L.tm_out, L.n, L.in_next, L.out,
+    k_stencil_tile<P, R, DT, STEPS, TH_><<<grid, THREADS, SMEM, L.stream>>>(L.tm_in, L.tm_out, L.n, L.in_next, L.out,
                                                                              L.status, L.depth, L.row0, L.goff,
                                                                              L.row0 + rows);
     return cudaGetLastError();

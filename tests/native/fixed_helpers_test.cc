@@ -137,6 +137,79 @@ int main()
         }
         std::printf("inc_whole checked=%ld certified=%ld\n", checked, certified);
     }
+    // The 96-bit fixed-point chain against the host's binary64 chain: fx96_from_bits of each term,
+    // fx96_acc_round for every add (or subtract), fx96_to_bits at the end, against
+    // ((p1 + p2) + ...) in binary64. Terms: products fl(w * v) of every PRK weight with whole numbers
+    // |v| < 2^20 (the stencil chains), and random multiples of 2^-62 below 2^20 with few significant
+    // bits, whose sums fall on rounding ties often. The domain is |sum| < 2^21 (the strict stencils'
+    // weights sum to at most 1.25 in magnitude and their values stay below 2^20); a chain is checked
+    // until it leaves it.
+    {
+        std::vector<double> ws;
+        for (int R = 1; R <= 5; ++R)
+            for (int m = 1; m <= R; ++m) {
+                ws.push_back(1.0 / (2.0 * m * R));
+                ws.push_back(1.0 / (4.0 * m * (2.0 * m - 1) * R));
+                ws.push_back(1.0 / (4.0 * m * R));
+            }
+        long checked = 0;
+        auto run_chain = [&](const std::vector<double>& terms, const std::vector<int>& neg) {
+            double want = neg[0] ? -terms[0] : terms[0];
+            uint32_t x0, x1, x2;
+            fx96_from_bits(bits(want), x0, x1, x2);
+            bool allneg0 = bits(want) == SIGN;
+            for (size_t k = 1; k < terms.size(); ++k) {
+                uint32_t p0, p1, p2;
+                fx96_from_bits(bits(terms[k]), p0, p1, p2);
+                if (neg[k]) {
+                    fx96_acc_round<true>(x0, x1, x2, p0, p1, p2);
+                    want = want - terms[k];
+                    allneg0 = allneg0 && bits(-terms[k]) == SIGN;
+                } else {
+                    fx96_acc_round<false>(x0, x1, x2, p0, p1, p2);
+                    want = want + terms[k];
+                    allneg0 = allneg0 && bits(terms[k]) == SIGN;
+                }
+                if (std::fabs(want) >= 0x1p21) break;  // outside the domain (the stencils stay below 2^21)
+                bad += fx96_to_bits(x0, x1, x2, allneg0) != bits(want);
+                ++checked;
+            }
+        };
+        for (int t = 0; t < 300000; ++t) {
+            const int len = 1 + static_cast<int>(g() % 110);
+            const int32_t vbase = static_cast<int32_t>(g() % (t % 3 == 0 ? 64 : (1u << 20)));
+            std::vector<double> terms;
+            std::vector<int> neg;
+            for (int k = 0; k < len; ++k) {
+                int32_t v = vbase + static_cast<int32_t>(g() % 200) - 100;
+                if (v <= -(1 << 20) || v >= (1 << 20)) v = 0;
+                const double w = ws[g() % ws.size()];
+                terms.push_back(w * static_cast<double>(v < 0 ? -v : v));
+                neg.push_back((v < 0) ^ static_cast<int>(g() & 1));
+            }
+            run_chain(terms, neg);
+        }
+        for (int t = 0; t < 300000; ++t) {
+            const int len = 2 + static_cast<int>(g() % 40);
+            std::vector<double> terms;
+            std::vector<int> neg;
+            for (int k = 0; k < len; ++k) {
+                const int sig = 1 + static_cast<int>(g() % 53);
+                const uint64_t mant = (g() >> (64 - sig)) | (1ull << (sig - 1));
+                const int e = static_cast<int>(g() % 30) - 10;  // leading bit 2^-10 .. 2^19
+                double v = std::ldexp(static_cast<double>(mant), e - (sig - 1));
+                if (g() % 17 == 0) v = 0.0;
+                terms.push_back(v);
+                neg.push_back(static_cast<int>(g() & 1));
+            }
+            run_chain(terms, neg);
+        }
+        // a chain of -0 terms, and cancellation to +0
+        run_chain({0.0, 0.0, 0.0}, {1, 1, 1});
+        run_chain({0.0, 0.0}, {1, 0});
+        run_chain({1.0 / 6.0 * 5, 1.0 / 6.0 * 5}, {0, 1});
+        std::printf("fx96 chain steps checked=%ld\n", checked);
+    }
     std::printf("bad=%d\n", bad);
     return bad != 0;
 }
