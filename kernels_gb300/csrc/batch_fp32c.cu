@@ -5,15 +5,15 @@
 namespace prk {
 namespace batch {
 
-PRK_BATCH_INSTANTIATE(FP32C, 1)
-PRK_BATCH_INSTANTIATE(FP32C, 2)
-PRK_BATCH_INSTANTIATE(FP32C, 4)
-PRK_BATCH_EXTERN(FP32C, 8)
-PRK_BATCH_EXTERN(FP32C, 0)
+PRK_BATCH_INSTANTIATE(FP32C, 1, FAM_ALL)
+PRK_BATCH_INSTANTIATE(FP32C, 2, FAM_ALL)
+PRK_BATCH_INSTANTIATE(FP32C, 4, FAM_ALL)
+PRK_BATCH_EXTERN(FP32C, 8, FAM_ALL)
+PRK_BATCH_EXTERN(FP32C, 0, FAM_ALL)
 
-cudaError_t launch_fp32c(int steps, const Launch& L) { return launch_depth<FP32C>(steps, L); }
+cudaError_t launch_fp32c(int steps, const Launch& L) { return launch_depth<FP32C, FAM_ALL>(steps, L); }
 
-int ctas_per_sm_fp32c(int steps) { return ctas_per_sm_depth<FP32C>(steps); }
+int ctas_per_sm_fp32c(int steps) { return ctas_per_sm_depth<FP32C, FAM_ALL>(steps); }
 
 }  // namespace batch
 }  // namespace prk

@@ -4,8 +4,8 @@
 namespace prk {
 namespace batch {
 
-PRK_BATCH_INSTANTIATE(FP32C, 8)
-PRK_BATCH_INSTANTIATE(FP32C, 0)
+PRK_BATCH_INSTANTIATE(FP32C, 8, FAM_ALL)
+PRK_BATCH_INSTANTIATE(FP32C, 0, FAM_ALL)
 
 }  // namespace batch
 }  // namespace prk

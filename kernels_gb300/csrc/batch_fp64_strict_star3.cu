@@ -1,0 +1,13 @@
+// The batched kernel for fp64 storage, family of the star stencil of radius 3 alone (its weights are
+// not powers of two: the table route), every temporal depth.
+#include "batch_kernel.cuh"
+
+namespace prk {
+namespace batch {
+
+cudaError_t launch_fp64_star3(int steps, const Launch& L) { return launch_depth<FP64, fam_one(STAR, 3)>(steps, L); }
+
+int ctas_per_sm_fp64_star3(int steps) { return ctas_per_sm_depth<FP64, fam_one(STAR, 3)>(steps); }
+
+}  // namespace batch
+}  // namespace prk

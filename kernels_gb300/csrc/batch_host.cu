@@ -23,13 +23,16 @@ int cuda_err(cudaError_t e, const char* what)
     return prk::record_error(static_cast<int>(e), msg);
 }
 
-// Grids advanced by one kernel sequence: all of one temporal depth.
+// Grids advanced by one kernel sequence: all of one kernel family (prk::batch::family_of) and one
+// temporal depth.
 struct Group {
+    int family = 0;
     int depth = 1;                     // applications per launch; 0: the rest of the run in one launch
     std::vector<int> members;          // indices into the batch's grid list
     GridDesc* d_desc = nullptr;        // device descriptors
     int64_t* d_off = nullptr;          // device tile offsets (members + 1)
     int64_t total = 0;                 // tiles over all members
+    int ctas = 0;                      // persistent CTAs per launch of this group's kernel
 };
 
 }  // namespace
@@ -39,12 +42,11 @@ struct prk_gb300_batch {
     std::vector<prk_gb300_grid> grids;
     std::vector<int> final_in;         // per grid, after the last run
     std::vector<Group> groups;
-    GridDesc* d_all = nullptr;         // all grids, for the depth-1 warm-up launch
-    int64_t* d_all_off = nullptr;
-    int64_t all_total = 0;
     unsigned long long* d_queue = nullptr;  // one work counter per launch of a run
     int queue_slots = 0;
-    int ctas = 0;                      // persistent CTAs per launch
+    std::vector<cudaStream_t> streams;  // one per group: the groups' launches run side by side
+    std::vector<cudaEvent_t> joins;     // one per group: its last launch done
+    cudaEvent_t fork = nullptr;
     std::map<int, cudaGraphExec_t> graphs;  // per iteration count
     int device = 0;
 };
@@ -93,12 +95,14 @@ int build_tables(prk_gb300_batch* b, const std::vector<int>& members, GridDesc**
     return PRK_OK;
 }
 
-// steps 1, 2, 4 or 8: a launch of that depth; steps 0: one launch of `apps` applications.
-cudaError_t launch_group(const prk_gb300_batch* b, const GridDesc* desc, const int64_t* off, int ngrids, int64_t total,
-                         int steps, int slot, int parity, cudaStream_t s, int apps = 0)
+// A launch of group g's kernel: steps 1, 2, 4 or 8, a launch of that depth; steps 0, one launch of
+// `apps` applications.
+cudaError_t launch_group(const prk_gb300_batch* b, const Group& g, int steps, int slot, int parity, cudaStream_t s,
+                         int apps = 0)
 {
-    prk::batch::Launch L{desc, off, ngrids, total, b->d_queue + slot, parity, b->ctas, s, apps};
-    return b->dtype == PRK_FP64 ? prk::batch::launch_fp64(steps, L) : prk::batch::launch_fp32c(steps, L);
+    prk::batch::Launch L{g.d_desc, g.d_off, static_cast<int>(g.members.size()), g.total, b->d_queue + slot, parity,
+                         g.ctas, s, apps};
+    return prk::batch::launch_family(b->dtype, g.family, steps, L);
 }
 
 // Applications of a group's next launch with `left` to go: the whole rest for depth 0, else the
@@ -119,25 +123,31 @@ int launches_of(const prk_gb300_batch* b, int iterations)
     return total;
 }
 
-// The timed part of a run: every group's launches for `iterations` applications. Slots 1.. of the
-// queue; group parities start at 1 (after the warm-up launch).
+// The timed part of a run: every group's launches for `iterations` applications, each group on its
+// own stream forked from and joined back into `s` (inside a capture this makes parallel branches of
+// the graph), so that different families' kernels share the GPU. Queue slots from the number of
+// groups on (the slots below are the warm-up's); group parities start at 1 (after the warm-up).
 int enqueue_timed(prk_gb300_batch* b, int iterations, cudaStream_t s, std::vector<int>* parity_out)
 {
-    int slot = 1;
+    int slot = static_cast<int>(b->groups.size());
     parity_out->assign(b->groups.size(), 1);
+    if (cudaError_t e = cudaEventRecord(b->fork, s)) return cuda_err(e, "cudaEventRecord");
     for (size_t gi = 0; gi < b->groups.size(); ++gi) {
         Group& g = b->groups[gi];
+        cudaStream_t gs = b->streams[gi];
+        if (cudaError_t e = cudaStreamWaitEvent(gs, b->fork, 0)) return cuda_err(e, "cudaStreamWaitEvent");
         int parity = 1, left = iterations;
         while (left > 0) {
             const int d = next_apps(g.depth, left);
             if (slot >= b->queue_slots) return err(PRK_ERR_STATE, "batch: more launches than queue slots");
-            cudaError_t e = launch_group(b, g.d_desc, g.d_off, static_cast<int>(g.members.size()), g.total,
-                                         g.depth == 0 ? 0 : d, slot++, parity, s, d);
+            cudaError_t e = launch_group(b, g, g.depth == 0 ? 0 : d, slot++, parity, gs, d);
             if (e != cudaSuccess) return cuda_err(e, "batch launch");
             parity ^= 1;
             left -= d;
         }
         (*parity_out)[gi] = parity;
+        if (cudaError_t e = cudaEventRecord(b->joins[gi], gs)) return cuda_err(e, "cudaEventRecord");
+        if (cudaError_t e = cudaStreamWaitEvent(s, b->joins[gi], 0)) return cuda_err(e, "cudaStreamWaitEvent");
     }
     return PRK_OK;
 }
@@ -169,8 +179,8 @@ int prk_gb300_batch_create(const prk_gb300_grid* grids, int count, int dtype, in
     b->final_in.assign(count, 0);
     if (cudaError_t e = cudaGetDevice(&b->device)) return cuda_err(e, "cudaGetDevice");
 
-    // group by temporal depth (tuned per grid, or one fixed depth)
-    std::map<int, std::vector<int>> by_depth;
+    // group by kernel family and temporal depth (tuned per grid, or one fixed depth)
+    std::map<std::pair<int, int>, std::vector<int>> by_key;
     for (int k = 0; k < count; ++k) {
         int d = depth;
         if (flags & PRK_BATCH_TUNED) {
@@ -178,27 +188,40 @@ int prk_gb300_batch_create(const prk_gb300_grid* grids, int count, int dtype, in
             if (int rc = prk_gb300_tune(grids[k].pattern, grids[k].radius, grids[k].n, dtype, PRK_TUNE_BATCH, &t)) return rc;
             d = t.depth;
         }
-        by_depth[d].push_back(k);
+        by_key[{prk::batch::family_of(dtype, grids[k].pattern, grids[k].radius), d}].push_back(k);
     }
-    for (auto& kv : by_depth) {
-        Group g;
-        g.depth = kv.first;
-        g.members = kv.second;
-        if (int rc = build_tables(b.get(), g.members, &g.d_desc, &g.d_off, &g.total)) return rc;
-        b->groups.push_back(std::move(g));
-    }
-    std::vector<int> all(count);
-    for (int k = 0; k < count; ++k) all[k] = k;
-    if (int rc = build_tables(b.get(), all, &b->d_all, &b->d_all_off, &b->all_total)) return rc;
-
-    int sms = 0, per = 0;
+    int sms = 0;
     if (cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device)) return cuda_err(e, "device query");
-    per = dtype == PRK_FP64 ? prk::batch::ctas_per_sm_fp64(1) : prk::batch::ctas_per_sm_fp32c(1);
-    b->ctas = sms * std::max(per, 1);
+    for (auto& kv : by_key) {
+        Group g;
+        g.family = kv.first.first;
+        g.depth = kv.first.second;
+        g.members = kv.second;
+        g.ctas = sms * std::max(prk::batch::ctas_per_sm_family(dtype, g.family, g.depth), 1);
+        const int rc = build_tables(b.get(), g.members, &g.d_desc, &g.d_off, &g.total);
+        b->groups.push_back(std::move(g));
+        if (rc) {
+            prk_gb300_batch_destroy(b.release());  // frees what was made so far
+            return rc;
+        }
+    }
+    auto fail_free = [&](int rc) {
+        prk_gb300_batch_destroy(b.release());
+        return rc;
+    };
+    for (size_t gi = 0; gi < b->groups.size(); ++gi) {
+        cudaStream_t st = nullptr;
+        cudaEvent_t ev = nullptr;
+        if (cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) return fail_free(cuda_err(e, "cudaStreamCreate"));
+        b->streams.push_back(st);
+        if (cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) return fail_free(cuda_err(e, "cudaEventCreate"));
+        b->joins.push_back(ev);
+    }
+    if (cudaError_t e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) return fail_free(cuda_err(e, "cudaEventCreate"));
     b->queue_slots = 4096;
     if (cudaMalloc(&b->d_queue, sizeof(unsigned long long) * b->queue_slots) != cudaSuccess) {
         cudaGetLastError();
-        return err(PRK_ERR_NOMEM, "batch: queue allocation failed");
+        return fail_free(err(PRK_ERR_NOMEM, "batch: queue allocation failed"));
     }
     *out = b.release();
     return PRK_OK;
@@ -208,7 +231,8 @@ int prk_gb300_batch_run(prk_gb300_batch* b, int iterations, int flags, double* e
 {
     if (!b) return err(PRK_ERR_ARG, "batch: null handle");
     if (iterations < 1) return err(PRK_ERR_ARG, "iterations must be >= 1");
-    if (launches_of(b, iterations) + 1 > b->queue_slots) return err(PRK_ERR_LIMIT, "batch: too many launches for one run");
+    if (launches_of(b, iterations) + static_cast<int>(b->groups.size()) > b->queue_slots)
+        return err(PRK_ERR_LIMIT, "batch: too many launches for one run");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     cudaStream_t own = nullptr;
     const bool graph = (flags & PRK_RUN_GRAPH) != 0;
@@ -223,16 +247,18 @@ int prk_gb300_batch_run(prk_gb300_batch* b, int iterations, int flags, double* e
     do {
         cudaError_t e;
         if ((e = cudaEventCreate(&e0)) != cudaSuccess || (e = cudaEventCreate(&e1)) != cudaSuccess) { rc = cuda_err(e, "cudaEventCreate"); break; }
-        // application 0 (untimed warm-up): one depth-1 launch over every grid, queue slot 0
+        // application 0 (untimed warm-up): one depth-1 launch per group, queue slots 0 .. groups - 1
+        const int ng = static_cast<int>(b->groups.size());
         if ((e = cudaMemsetAsync(b->d_queue, 0, sizeof(unsigned long long) * b->queue_slots, s)) != cudaSuccess) { rc = cuda_err(e, "queue reset"); break; }
-        if ((e = launch_group(b, b->d_all, b->d_all_off, static_cast<int>(b->grids.size()), b->all_total, 1, 0, 0, s)) != cudaSuccess) { rc = cuda_err(e, "batch warm-up launch"); break; }
+        for (int gi = 0; gi < ng && e == cudaSuccess; ++gi) e = launch_group(b, b->groups[gi], 1, gi, 0, s);
+        if (e != cudaSuccess) { rc = cuda_err(e, "batch warm-up launch"); break; }
         if (graph) {
             cudaGraphExec_t ge = nullptr;
             auto it = b->graphs.find(iterations);
             if (it == b->graphs.end()) {
                 cudaGraph_t g = nullptr;
                 if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) { rc = cuda_err(e, "cudaStreamBeginCapture"); break; }
-                rc = cudaMemsetAsync(b->d_queue + 1, 0, sizeof(unsigned long long) * (b->queue_slots - 1), s) == cudaSuccess
+                rc = cudaMemsetAsync(b->d_queue + ng, 0, sizeof(unsigned long long) * (b->queue_slots - ng), s) == cudaSuccess
                          ? enqueue_timed(b, iterations, s, &parity) : err(PRK_ERR_STATE, "queue reset during capture");
                 cudaError_t ec = cudaStreamEndCapture(s, &g);
                 if (rc != PRK_OK) { if (g) cudaGraphDestroy(g); break; }
@@ -318,8 +344,9 @@ int prk_gb300_batch_destroy(prk_gb300_batch* b)
         cudaFree(g.d_desc);
         cudaFree(g.d_off);
     }
-    cudaFree(b->d_all);
-    cudaFree(b->d_all_off);
+    for (cudaStream_t st : b->streams) cudaStreamDestroy(st);
+    for (cudaEvent_t ev : b->joins) cudaEventDestroy(ev);
+    if (b->fork) cudaEventDestroy(b->fork);
     cudaFree(b->d_queue);
     delete b;
     return PRK_OK;

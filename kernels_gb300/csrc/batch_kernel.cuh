@@ -31,20 +31,59 @@ struct GridDesc {
     int64_t tiles;
 };
 
-template <int DT>
+// Kernel families: the stencils one instantiation of the batched kernel evaluates, so that no kernel
+// carries the code and registers of stencils it does not run. FP32C: one family of every stencil.
+// FP64: the power-of-two stencils (star R=1,2 and grid R=1, the certified exact routes), and each
+// stencil with other weights on its own (the table route).
+constexpr int FAM_ALL = 0;
+constexpr int FAM_POW2 = 1;
+__host__ __device__ constexpr int fam_one(int P, int R) { return 16 + 8 * P + R; }
+
+__host__ __device__ constexpr bool in_family(int fam, int P, int R, int DT)
+{
+    if (fam == FAM_ALL) return DT == FP32C;
+    if (fam == FAM_POW2) return DT == FP64 && pow2_weights(P, R);
+    return DT == FP64 && fam == fam_one(P, R) && !pow2_weights(P, R);
+}
+
+// The family that evaluates a grid of (pattern, R) in storage form dtype.
+__host__ __device__ constexpr int family_of(int dtype, int P, int R)
+{
+    return dtype == FP32C ? FAM_ALL : (pow2_weights(P, R) ? FAM_POW2 : fam_one(P, R));
+}
+
+template <int DT, int FAM>
 constexpr int max_in_bytes()
 {
     int m = 0;
-#define PRK_MAXB(RR) m = tile::Geo<DT, RR>::IN_BYTES > m ? tile::Geo<DT, RR>::IN_BYTES : m;
-    PRK_MAXB(1) PRK_MAXB(2) PRK_MAXB(3) PRK_MAXB(4) PRK_MAXB(5)
+    for (int P = 0; P < 2; ++P) {
+#define PRK_MAXB(RR) \
+    if (in_family(FAM, P, RR, DT) && tile::Geo<DT, RR>::IN_BYTES > m) m = tile::Geo<DT, RR>::IN_BYTES;
+        PRK_MAXB(1) PRK_MAXB(2) PRK_MAXB(3) PRK_MAXB(4) PRK_MAXB(5)
 #undef PRK_MAXB
+    }
     return m;
 }
 
-template <int DT>
+template <int DT, int FAM>
+constexpr int max_table_bytes()
+{
+    int m = 0;
+#define PRK_MAXT(PP, RR) \
+    if (in_family(FAM, PP, RR, DT) && tile::table_bytes<PP, RR, DT>() > m) m = tile::table_bytes<PP, RR, DT>();
+    PRK_MAXT(STAR, 1) PRK_MAXT(STAR, 2) PRK_MAXT(STAR, 3) PRK_MAXT(STAR, 4) PRK_MAXT(STAR, 5)
+    PRK_MAXT(GRID, 1) PRK_MAXT(GRID, 2) PRK_MAXT(GRID, 3) PRK_MAXT(GRID, 4) PRK_MAXT(GRID, 5)
+#undef PRK_MAXT
+    return m;
+}
+
+// Shared memory: the staged `in` tile, the reduction words, and the table route's product tables.
+template <int DT, int FAM>
 struct Layout {
-    static constexpr int RED_OFF = (max_in_bytes<DT>() + 127) / 128 * 128;
-    static constexpr int SMEM = RED_OFF + tile::WARPS * 8;
+    static constexpr int RED_OFF = (max_in_bytes<DT, FAM>() + 127) / 128 * 128;
+    static constexpr int TBL_OFF = (RED_OFF + tile::WARPS * 8 + 15) / 16 * 16;
+    static constexpr int SMEM = TBL_OFF + max_table_bytes<DT, FAM>();
+    static_assert(SMEM <= tile::SMEM_PER_CTA_MAX, "the tile and its tables must fit in shared memory");
 };
 
 // Stage the `in` tile at (i0, j0) with its halo in shared memory: coalesced plain loads, zero
@@ -90,10 +129,10 @@ __device__ __forceinline__ void stage_tile(unsigned char* smem, const void* in_v
     __syncthreads();
 }
 
-// One work item: load the tile of grid g at `parity`, then evaluate it.
+// One work item: load the tile of grid g at `parity`, then evaluate it. tbl: the table area.
 template <int P, int R, int DT, int STEPS>
 __device__ __forceinline__ void item(unsigned char* smem, int* s_red, const GridDesc& g, int64_t t, int parity,
-                                     int depth)
+                                     int depth, unsigned char* tbl)
 {
     using C = tile::Cfg<DT>;
     const int64_t n = g.n;
@@ -101,15 +140,18 @@ __device__ __forceinline__ void item(unsigned char* smem, int* s_red, const Grid
     const int64_t j0 = (t % g.tiles_x) * C::TW;
     stage_tile<R, DT>(smem, g.in[parity], n, n, i0, j0);
     tile::process_tile<P, R, DT, STEPS, tile::OUT_HBM>(smem, s_red, i0, j0, n, tile::tile_has_out(i0, j0, n, R, C::TW, C::TH),
-                                               g.in[parity ^ 1], g.out, g.vec_ok != 0, depth, 0, n);
+                                               g.in[parity ^ 1], g.out, g.vec_ok != 0, depth, 0, n,
+                                               tile::table_route<P, R, DT>() ? tbl : nullptr);
 }
 
-template <int DT, int STEPS>
+template <int DT, int STEPS, int FAM>
 __device__ __forceinline__ void dispatch(unsigned char* smem, int* s_red, const GridDesc& g, int64_t t, int parity,
-                                         int depth)
+                                         int depth, unsigned char* tbl)
 {
-#define PRK_ITEM(PP, RR) \
-    case RR: item<PP, RR, DT, STEPS>(smem, s_red, g, t, parity, depth); break;
+#define PRK_ITEM(PP, RR)                                                                  \
+    case RR:                                                                              \
+        if constexpr (in_family(FAM, PP, RR, DT)) item<PP, RR, DT, STEPS>(smem, s_red, g, t, parity, depth, tbl); \
+        break;
     if (g.pattern == STAR) {
         switch (g.R) { PRK_ITEM(STAR, 1) PRK_ITEM(STAR, 2) PRK_ITEM(STAR, 3) PRK_ITEM(STAR, 4) PRK_ITEM(STAR, 5) }
     } else {
@@ -118,14 +160,14 @@ __device__ __forceinline__ void dispatch(unsigned char* smem, int* s_red, const 
 #undef PRK_ITEM
 }
 
-template <int DT, int STEPS>
+template <int DT, int STEPS, int FAM>
 __global__ void __launch_bounds__(tile::THREADS, 2)
     k_batch(const GridDesc* __restrict__ grids, const int64_t* __restrict__ tile_off, int ngrids, int64_t total,
             unsigned long long* __restrict__ queue, int parity, int depth)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ long long s_item;
-    int* s_red = reinterpret_cast<int*>(smem + Layout<DT>::RED_OFF);
+    int* s_red = reinterpret_cast<int*>(smem + Layout<DT, FAM>::RED_OFF);
     for (;;) {
         if (threadIdx.x == 0) s_item = static_cast<long long>(atomicAdd(queue, 1ull));
         __syncthreads();
@@ -138,7 +180,7 @@ __global__ void __launch_bounds__(tile::THREADS, 2)
             else hi = mid;
         }
         const GridDesc g = grids[lo];
-        dispatch<DT, STEPS>(smem, s_red, g, it - tile_off[lo], parity, depth);
+        dispatch<DT, STEPS, FAM>(smem, s_red, g, it - tile_off[lo], parity, depth, smem + Layout<DT, FAM>::TBL_OFF);
         __syncthreads();  // shared memory and s_item are reused by the next item
     }
 }
@@ -155,67 +197,87 @@ struct Launch {
     int depth;  // applications of a run-time-depth launch (STEPS = 0)
 };
 
-template <int DT, int STEPS>
+template <int DT, int STEPS, int FAM>
 cudaError_t launch(const Launch& L)
 {
-    if (cudaError_t e = cudaFuncSetAttribute(k_batch<DT, STEPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, Layout<DT>::SMEM))
+    constexpr int SM = Layout<DT, FAM>::SMEM;
+    if (cudaError_t e = cudaFuncSetAttribute(k_batch<DT, STEPS, FAM>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM))
         return e;
     if (STEPS == 0 && L.depth < 1) return cudaErrorInvalidValue;
-    k_batch<DT, STEPS><<<L.ctas, tile::THREADS, Layout<DT>::SMEM, L.stream>>>(L.grids, L.tile_off, L.ngrids, L.total,
-                                                                             L.queue, L.parity, L.depth);
+    k_batch<DT, STEPS, FAM><<<L.ctas, tile::THREADS, SM, L.stream>>>(L.grids, L.tile_off, L.ngrids, L.total, L.queue,
+                                                                      L.parity, L.depth);
     return cudaGetLastError();
 }
 
-// Resident CTAs per SM of k_batch<DT, STEPS> (occupancy query; 0 on failure).
-template <int DT, int STEPS>
+// Resident CTAs per SM of k_batch<DT, STEPS, FAM> (occupancy query; 0 on failure).
+template <int DT, int STEPS, int FAM>
 int ctas_per_sm()
 {
+    constexpr int SM = Layout<DT, FAM>::SMEM;
     int b = 0;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<DT, STEPS>, tile::THREADS, Layout<DT>::SMEM) == cudaSuccess
+    if (cudaFuncSetAttribute(k_batch<DT, STEPS, FAM>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM) != cudaSuccess) return 0;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch<DT, STEPS, FAM>, tile::THREADS, SM) == cudaSuccess
                ? b : 0;
 }
 
-// Each (form, depth) pair is instantiated in one translation unit (batch_fp64*.cu, batch_fp32c*.cu)
-// so that the build compiles them in parallel; the dispatching units declare them with this.
-#define PRK_BATCH_EXTERN(DT, S)                                  \
-    extern template cudaError_t launch<DT, S>(const Launch& L); \
-    extern template int ctas_per_sm<DT, S>();
-#define PRK_BATCH_INSTANTIATE(DT, S)                      \
-    template cudaError_t launch<DT, S>(const Launch& L); \
-    template int ctas_per_sm<DT, S>();
-
-template <int DT>
+template <int DT, int FAM>
 cudaError_t launch_depth(int steps, const Launch& L)
 {
     switch (steps) {
-    case 1: return launch<DT, 1>(L);
-    case 2: return launch<DT, 2>(L);
-    case 4: return launch<DT, 4>(L);
-    case 8: return launch<DT, 8>(L);
-    case 0: return launch<DT, 0>(L);
+    case 1: return launch<DT, 1, FAM>(L);
+    case 2: return launch<DT, 2, FAM>(L);
+    case 4: return launch<DT, 4, FAM>(L);
+    case 8: return launch<DT, 8, FAM>(L);
+    case 0: return launch<DT, 0, FAM>(L);
     }
     return cudaErrorInvalidValue;
 }
 
-template <int DT>
+template <int DT, int FAM>
 int ctas_per_sm_depth(int steps)
 {
     switch (steps) {
-    case 1: return ctas_per_sm<DT, 1>();
-    case 2: return ctas_per_sm<DT, 2>();
-    case 4: return ctas_per_sm<DT, 4>();
-    case 8: return ctas_per_sm<DT, 8>();
-    case 0: return ctas_per_sm<DT, 0>();
+    case 1: return ctas_per_sm<DT, 1, FAM>();
+    case 2: return ctas_per_sm<DT, 2, FAM>();
+    case 4: return ctas_per_sm<DT, 4, FAM>();
+    case 8: return ctas_per_sm<DT, 8, FAM>();
+    case 0: return ctas_per_sm<DT, 0, FAM>();
     }
     return 0;
 }
 
-// Per-form entry points (batch_fp64.cu, batch_fp32c.cu).
-cudaError_t launch_fp64(int steps, const Launch& L);
+// Per-family entry points, one translation unit each so that the build compiles them in parallel:
+// batch_fp64_pow2.cu, batch_fp64_strict_*.cu (one per stencil with other weights) and the FP32C
+// depths (batch_fp32c.cu with batch_fp32c_deep.cu).
+cudaError_t launch_fp64_pow2(int steps, const Launch& L);
+int ctas_per_sm_fp64_pow2(int steps);
+#define PRK_BATCH_STRICT_DECL(PN, RR)                                 \
+    cudaError_t launch_fp64_##PN##RR(int steps, const Launch& L); \
+    int ctas_per_sm_fp64_##PN##RR(int steps);
+PRK_BATCH_STRICT_DECL(star, 3)
+PRK_BATCH_STRICT_DECL(star, 4)
+PRK_BATCH_STRICT_DECL(star, 5)
+PRK_BATCH_STRICT_DECL(grid, 2)
+PRK_BATCH_STRICT_DECL(grid, 3)
+PRK_BATCH_STRICT_DECL(grid, 4)
+PRK_BATCH_STRICT_DECL(grid, 5)
+#undef PRK_BATCH_STRICT_DECL
+
+// The FP32C depths are instantiated in two translation units; the dispatching unit declares the
+// other's with this.
+#define PRK_BATCH_EXTERN(DT, S, F)                                  \
+    extern template cudaError_t launch<DT, S, F>(const Launch& L); \
+    extern template int ctas_per_sm<DT, S, F>();
+#define PRK_BATCH_INSTANTIATE(DT, S, F)                      \
+    template cudaError_t launch<DT, S, F>(const Launch& L); \
+    template int ctas_per_sm<DT, S, F>();
+
 cudaError_t launch_fp32c(int steps, const Launch& L);
-// Resident CTAs per SM of the batched kernel at a depth (occupancy query; 0 on failure).
-int ctas_per_sm_fp64(int steps);
 int ctas_per_sm_fp32c(int steps);
+
+// Dispatch by family (host side): a grid's family as family_of gives it.
+cudaError_t launch_family(int dtype, int fam, int steps, const Launch& L);
+int ctas_per_sm_family(int dtype, int fam, int steps);
 
 }  // namespace batch
 }  // namespace prk

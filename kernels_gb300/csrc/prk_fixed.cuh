@@ -15,6 +15,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstring>
 
 #ifdef __CUDACC__
 #define PRK_HD __host__ __device__ __forceinline__
@@ -173,6 +174,28 @@ PRK_HD uint64_t mul_whole20(uint64_t wb, int32_t v)
 // with the same bits (fx96_to_bits).
 constexpr int FX96_F = 62;
 
+PRK_HD float f32_from_bits(uint32_t u)
+{
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(u);
+#else
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+#endif
+}
+
+PRK_HD uint32_t f32_bits(float f)
+{
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(f);
+#else
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+#endif
+}
+
 // x = v * 2^62 for a binary64 v (encoding b) with |v| < 2^22 that is a multiple of 2^-62, or +-0.
 PRK_HD void fx96_from_bits(uint64_t b, uint32_t& x0, uint32_t& x1, uint32_t& x2)
 {
@@ -226,24 +249,31 @@ PRK_HD void fx96_acc_round(uint32_t& x0, uint32_t& x1, uint32_t& x2, uint32_t p0
     x0 = static_cast<uint32_t>(r);
     x1 = static_cast<uint32_t>(r >> 32);
 #endif
+    // b = max(0, msb|sum| - 52). The leading bit is read from the one's complement of a negative sum
+    // (t2:t1 below), and its position from the exponent of an exact float: float(t2) when the high
+    // word is not zero (t2 < 2^20: b = msb(t2) + 12), else float(t1 >> 9) (b = msb(t1 >> 9) - 11, and 0
+    // for anything smaller), each converted with the 2^23 magic number (no leading-zero count, which
+    // issues at a quarter of the integer rate).
     const uint32_t sg = static_cast<uint32_t>(static_cast<int32_t>(x2) >> 31);
     const uint32_t t2 = x2 ^ sg, t1 = x1 ^ sg;
-    int b = t2 ? 43 - clz32(t2) : 11 - clz32(t1);
-    b = b < 0 ? 0 : b;
+    const uint32_t y = t2 ? t2 : (t1 >> 9);
+    const int off = t2 ? 115 : 138;
+    const int b0 = static_cast<int>(f32_bits(f32_from_bits(0x4B000000u | y) - 8388608.0f) >> 23) - off;
+    const int b = b0 < 0 ? 0 : b0;
+    // round to a multiple of 2^b, nearest-even: add 2^(b-1) - 1 and the lowest kept bit, then cut
     const uint32_t mask = (1u << b) - 1u;
-    const uint32_t q = (x0 >> b) & (mask & 1u);  // lowest kept bit; 0 when nothing is cut
-    const uint32_t inc = (((x0 & mask) + (mask >> 1) + q) >> b) << b;
-    const uint32_t cut = x0 & ~mask;
+    const uint32_t hq = (mask >> 1) + ((x0 >> b) & (mask & 1u));
 #ifdef __CUDA_ARCH__
-    asm("add.cc.u32 %0, %3, %4;\n\taddc.cc.u32 %1, %1, 0;\n\taddc.u32 %2, %2, 0;"
-        : "=r"(x0), "+r"(x1), "+r"(x2)
-        : "r"(cut), "r"(inc));
+    asm("add.cc.u32 %0, %0, %3;\n\taddc.cc.u32 %1, %1, 0;\n\taddc.u32 %2, %2, 0;"
+        : "+r"(x0), "+r"(x1), "+r"(x2)
+        : "r"(hq));
 #else
-    const uint64_t old = (static_cast<uint64_t>(x1) << 32) | cut, lo = old + inc;
+    const uint64_t old = (static_cast<uint64_t>(x1) << 32) | x0, lo = old + hq;
     x2 += lo < old ? 1u : 0u;
     x0 = static_cast<uint32_t>(lo);
     x1 = static_cast<uint32_t>(lo >> 32);
 #endif
+    x0 &= ~mask;
 }
 
 // The binary64 encoding of x * 2^-62 for a value with at most 53 significant bits (a rounded sum)

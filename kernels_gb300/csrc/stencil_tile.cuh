@@ -695,9 +695,15 @@ __device__ __forceinline__ void advance_i32(int32_t* p)
     }
 }
 
+// Where process_tile finds `out`: the out tile loaded into shared memory next to `in` (TMA path), or
+// HBM, read in the evaluation row by row (batched path) or with every row's words requested before
+// the first row is evaluated (plain-staged path; used for the FP64 power-of-two stencils at one
+// application, where it measured faster, and like OUT_HBM otherwise).
+constexpr int OUT_SMEM = 0, OUT_HBM = 1, OUT_HBM_AHEAD = 2;
+
 // ---------------------------------------------------------------------------------------------
 // FP64 stencils whose weights are not powers of two, on whole-number tiles of small range: the
-// table route (TMA tiles only).
+// table route.
 //
 // Every product and every partial sum of the reference's chain rounds, and GB300 issues binary64
 // adds at a small fraction of its integer rate, so the route moves work off the binary64 pipe
@@ -765,15 +771,19 @@ static_assert(strict_taps_ok<STAR, 3>() && strict_taps_ok<STAR, 4>() && strict_t
                   strict_taps_ok<GRID, 5>(),
               "strict tap groups");
 
-// Sixteenths of each chain that run in fixed point (the rest stays on the binary64 pipe).
-#ifndef PRK_FX_SIXTEENTHS
-#define PRK_FX_SIXTEENTHS 11
+// Sixteenths of each chain that run in fixed point (the rest stays on the binary64 pipe), per
+// pattern, as measured best at n=16384 (star 11, grid 9; 7 to 13 were within a few percent).
+#ifndef PRK_FX_SIXTEENTHS_STAR
+#define PRK_FX_SIXTEENTHS_STAR 11
+#endif
+#ifndef PRK_FX_SIXTEENTHS_GRID
+#define PRK_FX_SIXTEENTHS_GRID 9
 #endif
 
 template <int P, int R>
 constexpr int fixed_taps()
 {
-    const int k = tap_count(P, R) * PRK_FX_SIXTEENTHS / 16;
+    const int k = tap_count(P, R) * (P == STAR ? PRK_FX_SIXTEENTHS_STAR : PRK_FX_SIXTEENTHS_GRID) / 16;
     return k < 1 ? 1 : (k > tap_count(P, R) ? tap_count(P, R) : k);
 }
 
@@ -837,107 +847,98 @@ __device__ __forceinline__ void fx96_tap(uint32_t (&x)[3], const uint4& p, int n
         fx::fx96_acc_round<false>(x[0], x[1], x[2], p.x, p.y, p.z);
 }
 
-// One application to the points (r, c) and (r, c + 32) of the thread's rows: the reference chain of
-// each point, then out += S, into the shared-memory out tile. si points at the int32 tile's (0, 0)
-// (row stride SW), o_tile is the out tile (row stride TW). Only the interior points are written.
-template <int P, int R, int SW, int TW, int ROWS>
-__device__ __forceinline__ void table_application(const int32_t* si, uint64_t* o_tile, const uint64_t* T64,
-                                                  const uint4* T96, int base, int64_t i0, int64_t j0, int64_t n,
-                                                  int64_t goff, int64_t row_end, bool has_out)
+// Where a row of the table route's points lies: a row whose points are all outside the interior or
+// past row_end is skipped (row-uniform); a column outside the interior is computed and dropped.
+__device__ __forceinline__ bool table_row_active(bool has_out, int64_t gi, int64_t gg, int64_t row_end, int64_t n, int R)
+{
+    return has_out && gi < row_end && gg >= R && gg < n - R;
+}
+
+// The chain S of the points (r, c) and (r, c + 32): the reference's sum of fl(w * v) over the taps in
+// the generator's order, its first fixed_taps() adds in fixed point. sp points at the int32 tile's
+// (r, c) (row stride SW); the tables cover [base, base + TBL_L).
+template <int P, int R, int SW>
+__device__ __forceinline__ void table_chain(const int32_t* sp, const uint64_t* T64, const uint4* T96, int base,
+                                            double (&d)[2])
 {
     constexpr StrictTaps<P, R> TP = make_strict_taps<P, R>();
     constexpr int N = tap_count(P, R), KF = fixed_taps<P, R>();
     constexpr bool POS = fixed_prefix_has_positive<P, R>();
-    static_assert(TW == 64, "two columns per lane, 32 apart");
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll 1
-    for (int rr = 0; rr < ROWS; ++rr) {
-        const int r = warp * ROWS + rr;
-        const int64_t gi = i0 + r, gg = gi + goff;
-        if (!has_out || gi >= row_end || gg < R || gg >= n - R) continue;  // warp-uniform
-        const int32_t* sp = si + r * SW + lane;
-        uint32_t x[2][3];
-        int anyv[2] = {0, 0};
+    uint32_t x[2][3];
+    int anyv[2] = {0, 0};
 #pragma unroll
-        for (int t = 0; t < KF; ++t) {
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int v = sp[TP.dr[t] * SW + TP.dc[t] + 32 * h];
-                if (!POS) anyv[h] |= v;
-                const uint4 p = T96[TP.g[t] * TBL_L + (v - base)];
-                if (t == 0) {
-                    if (TP.neg[t]) {  // x = -p, the 96-bit two's-complement negation
-                        x[h][0] = ~p.x + 1u;
-                        x[h][1] = ~p.y + (p.x == 0u ? 1u : 0u);
-                        x[h][2] = ~p.z + ((p.x | p.y) == 0u ? 1u : 0u);
-                    } else {
-                        x[h][0] = p.x;
-                        x[h][1] = p.y;
-                        x[h][2] = p.z;
-                    }
-                } else {
-                    fx96_tap(x[h], p, TP.neg[t]);
-                }
-            }
-        }
-        double d[2];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) d[h] = as_dbl(fx::fx96_to_bits(x[h][0], x[h][1], x[h][2], !POS && anyv[h] == 0));
-#pragma unroll
-        for (int t = KF; t < N; ++t) {
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int v = sp[TP.dr[t] * SW + TP.dc[t] + 32 * h];
-                const double p = as_dbl(T64[TP.g[t] * TBL_L + (v - base)]);
-                d[h] = TP.neg[t] ? __dsub_rn(d[h], p) : __dadd_rn(d[h], p);
-            }
-        }
+    for (int t = 0; t < KF; ++t) {
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-            const int c = lane + 32 * h;
-            const int64_t gj = j0 + c;
-            if (gj >= R && gj < n - R) o_tile[r * TW + c] = as_bits(__dadd_rn(as_dbl(o_tile[r * TW + c]), d[h]));
+            const int v = sp[TP.dr[t] * SW + TP.dc[t] + 32 * h];
+            if (!POS) anyv[h] |= v;
+            const uint4 p = T96[TP.g[t] * TBL_L + (v - base)];
+            if (t == 0) {
+                if (TP.neg[t]) {  // x = -p, the 96-bit two's-complement negation
+                    x[h][0] = ~p.x + 1u;
+                    x[h][1] = ~p.y + (p.x == 0u ? 1u : 0u);
+                    x[h][2] = ~p.z + ((p.x | p.y) == 0u ? 1u : 0u);
+                } else {
+                    x[h][0] = p.x;
+                    x[h][1] = p.y;
+                    x[h][2] = p.z;
+                }
+            } else {
+                fx96_tap(x[h], p, TP.neg[t]);
+            }
+        }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) d[h] = as_dbl(fx::fx96_to_bits(x[h][0], x[h][1], x[h][2], !POS && anyv[h] == 0));
+#pragma unroll
+    for (int t = KF; t < N; ++t) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int v = sp[TP.dr[t] * SW + TP.dc[t] + 32 * h];
+            const double p = as_dbl(T64[TP.g[t] * TBL_L + (v - base)]);
+            d[h] = TP.neg[t] ? __dsub_rn(d[h], p) : __dadd_rn(d[h], p);
         }
     }
 }
 
-// The table route for a whole tile: `nsteps` applications into the out tile, with the int32 tile
-// (holding the tile's in, halo included) advanced in place between them, as the other routes leave
-// it for the stores. Returns false, having done nothing, when the tile's values span TBL_L or more
-// (block-uniform; s_red holds two ints per warp).
-template <int P, int R, int SW, int SH, int TW, int ROWS>
-__device__ __forceinline__ bool table_tile(int32_t* si, uint64_t* o_tile, unsigned char* tbl, int* s_red, int nsteps,
-                                           int64_t i0, int64_t j0, int64_t n, int64_t goff, int64_t row_end,
-                                           bool has_out)
+// The table route for a whole tile whose int32 values (the tile's in, halo included) lie in
+// [lo, hi]: `nsteps` applications, with the int32 tile advanced in place between them, as the other
+// routes leave it for the stores. Lane l owns columns l and l + 32 of its warp's rows; their out
+// words stay in registers across the applications, read from and written back to the shared-memory
+// out tile (OUT_SMEM) or the out array itself (the other sources: out_g points at the tile's (0, 0),
+// row stride n). Returns false, having done nothing, when the values span TBL_L or more (lo and hi
+// are block-uniform).
+template <int P, int R, int SW, int SH, int TW, int ROWS, int OUT_SRC>
+__device__ __forceinline__ bool table_tile(int32_t* si, uint64_t* o_tile, uint64_t* out_g, unsigned char* tbl, int lo,
+                                           int hi, int nsteps, int64_t i0, int64_t j0, int64_t n, int64_t goff,
+                                           int64_t row_end, bool has_out)
 {
     constexpr int ELEMS = SW * SH;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int lo = 0x7FFFFFFF, hi = -0x7FFFFFFF;
-    for (int idx = threadIdx.x; idx < ELEMS; idx += THREADS) {
-        lo = min(lo, si[idx]);
-        hi = max(hi, si[idx]);
-    }
-    lo = __reduce_min_sync(0xffffffffu, lo);
-    hi = __reduce_max_sync(0xffffffffu, hi);
-    if (lane == 0) {
-        s_red[2 * warp] = lo;
-        s_red[2 * warp + 1] = hi;
-    }
-    __syncthreads();
-    lo = s_red[0];
-    hi = s_red[1];
-#pragma unroll
-    for (int w = 1; w < WARPS; ++w) {
-        lo = min(lo, s_red[2 * w]);
-        hi = max(hi, s_red[2 * w + 1]);
-    }
-    __syncthreads();  // s_red read by every thread before anyone reuses it
+    static_assert(TW == 64, "two columns per lane, 32 apart");
     if (hi - lo >= TBL_L) return false;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint64_t* T64 = reinterpret_cast<uint64_t*>(tbl);
     uint4* T96 = reinterpret_cast<uint4*>(tbl + group_count<P, R>() * TBL_L * 8);
     int base = lo;
     build_tables<P, R>(T64, T96, base);
-    __syncthreads();
+    // the thread's out words
+    uint64_t o[ROWS][2];
+#pragma unroll
+    for (int rr = 0; rr < ROWS; ++rr) {
+        const int r = warp * ROWS + rr;
+        const int64_t gi = i0 + r;
+        const bool act = table_row_active(has_out, gi, gi + goff, row_end, n, R);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int c = lane + 32 * h;
+            const bool col = j0 + c >= R && j0 + c < n - R;
+            if constexpr (OUT_SRC == OUT_SMEM)
+                o[rr][h] = act ? o_tile[r * TW + c] : 0ull;
+            else
+                o[rr][h] = act && col ? out_g[r * n + c] : 0ull;
+        }
+    }
+    __syncthreads();  // the tables complete
     const int32_t* s0 = si + R * SW + ((SW - TW) / 2);  // the tile's (0, 0)
 #pragma unroll 1
     for (int t = 0; t < nsteps; ++t) {
@@ -949,8 +950,33 @@ __device__ __forceinline__ bool table_tile(int32_t* si, uint64_t* o_tile, unsign
             }
             __syncthreads();
         }
-        table_application<P, R, SW, TW, ROWS>(s0, o_tile, T64, T96, base, i0, j0, n, goff, row_end, has_out);
+#pragma unroll 1
+        for (int rr = 0; rr < ROWS; ++rr) {
+            const int r = warp * ROWS + rr;
+            const int64_t gi = i0 + r;
+            if (!table_row_active(has_out, gi, gi + goff, row_end, n, R)) continue;  // warp-uniform
+            double d[2];
+            table_chain<P, R, SW>(s0 + r * SW + lane, T64, T96, base, d);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) o[rr][h] = as_bits(__dadd_rn(as_dbl(o[rr][h]), d[h]));
+        }
         if (t + 1 < nsteps) __syncthreads();  // every thread's reads done before the next advance
+    }
+#pragma unroll
+    for (int rr = 0; rr < ROWS; ++rr) {
+        const int r = warp * ROWS + rr;
+        const int64_t gi = i0 + r;
+        if (!table_row_active(has_out, gi, gi + goff, row_end, n, R)) continue;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int c = lane + 32 * h;
+            if (j0 + c >= R && j0 + c < n - R) {
+                if constexpr (OUT_SRC == OUT_SMEM)
+                    o_tile[r * TW + c] = o[rr][h];
+                else
+                    out_g[r * n + c] = o[rr][h];
+            }
+        }
     }
     __syncthreads();  // the out tile complete before the stores read it in their layout
     return true;
@@ -965,11 +991,6 @@ __device__ __forceinline__ bool tile_has_out(int64_t i0, int64_t j0, int64_t n, 
     return (i0 + th > R) && (i0 < n - R) && (j0 + tw > R) && (j0 < n - R);
 }
 
-// Where process_tile finds `out`: the out tile loaded into shared memory next to `in` (TMA path), or
-// HBM, read in the evaluation row by row (batched path) or with every row's words requested before
-// the first row is evaluated (plain-staged path; used for the FP64 power-of-two stencils at one
-// application, where it measured faster, and like OUT_HBM otherwise).
-constexpr int OUT_SMEM = 0, OUT_HBM = 1, OUT_HBM_AHEAD = 2;
 
 // Evaluate one tile whose `in` (with halo) is in shared memory: STEPS applications (`depth` when
 // STEPS = 0), then in_next and out to HBM, with out read from OUT_SRC. vec_ok: rows are 16-byte
@@ -981,7 +1002,8 @@ constexpr int OUT_SMEM = 0, OUT_HBM = 1, OUT_HBM_AHEAD = 2;
 template <int P, int R, int DT, int STEPS, int OUT_SRC = OUT_SMEM, int TH_ = 32>
 __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, int64_t i0, int64_t j0, int64_t n,
                                              bool has_out, void* __restrict__ in_next_v, void* __restrict__ out_v,
-                                             bool vec_ok, int depth, int64_t goff, int64_t row_end)
+                                             bool vec_ok, int depth, int64_t goff, int64_t row_end,
+                                             unsigned char* tbl)
 {
     const int nsteps = STEPS > 0 ? STEPS : depth;
     using G = Geo<DT, R, TH_>;
@@ -1102,6 +1124,23 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
             iv[q] = b == 0ull ? 0 : ((b >> 63) ? -a : a);
             ok = ok && (b == 0ull || whole);
         }
+        if constexpr (table_route<P, R, DT>()) {
+            // the tile's range for the table route, published with the certification's barrier
+            int lo = 0x7FFFFFFF, hi = -0x7FFFFFFF;
+#pragma unroll
+            for (int q = 0; q < PER; ++q) {
+                if (threadIdx.x + q * THREADS < G::ELEMS) {
+                    lo = min(lo, iv[q]);
+                    hi = max(hi, iv[q]);
+                }
+            }
+            lo = __reduce_min_sync(0xffffffffu, lo);
+            hi = __reduce_max_sync(0xffffffffu, hi);
+            if (lane == 0) {
+                s_red[2 * warp] = lo;
+                s_red[2 * warp + 1] = hi;
+            }
+        }
         iwhole = __syncthreads_and(ok) != 0;
         if (iwhole) {
             int32_t* si = reinterpret_cast<int32_t*>(s_in);
@@ -1114,14 +1153,25 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
         __syncthreads();
     }
 
-    // ---- FP64, other weights, TMA tiles: the table route (table_tile), when the range allows ----
+    // ---- FP64, other weights: the table route (table_tile), when the kernel has a table area and
+    // the tile's range fits it ----
     bool tbl_done = false;
-    if constexpr (table_route<P, R, DT>() && OUT_SRC == OUT_SMEM) {
-        if (iwhole)
-            tbl_done = table_tile<P, R, G::SW, G::SH, C::TW, ROWS>(reinterpret_cast<int32_t*>(s_in), o_tile,
-                                                                   stage + table_offset<DT, R, TH_>(), s_red, nsteps,
-                                                                   i0, j0, n, goff, row_end, has_out);
+    if constexpr (table_route<P, R, DT>()) {
+        if (iwhole && tbl) {
+            int lo = s_red[0], hi = s_red[1];
+#pragma unroll
+            for (int w = 1; w < WARPS; ++w) {
+                lo = min(lo, s_red[2 * w]);
+                hi = max(hi, s_red[2 * w + 1]);
+            }
+            tbl_done = table_tile<P, R, G::SW, G::SH, C::TW, ROWS, OUT_SRC>(
+                reinterpret_cast<int32_t*>(s_in), o_tile, static_cast<uint64_t*>(out_v) + i0 * n + j0, tbl, lo, hi,
+                nsteps, i0, j0, n, goff, row_end, has_out);
+        }
     }
+
+    // The table route with out in HBM has stored out itself; the stores then write in_next only
+    const bool out_via_rows = !(tbl_done && OUT_SRC != OUT_SMEM);
 
     // Set by the multi-application FP32 route when the tile's out words are held as integers
     bool oint = false;
@@ -1284,7 +1334,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
             const int r = warp * ROWS + rr;
             const int64_t gi = i0 + r, gg = gi + goff;
             if (!col_ok || gi >= row_end) continue;
-            const bool row_out = has_out && gg >= R && gg < n - R;
+            const bool row_out = out_via_rows && has_out && gg >= R && gg < n - R;
             uint64_t o[CPT];
             if (row_out) {
 #pragma unroll
@@ -1307,7 +1357,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
         for (int rr = 0; rr < ROWS; ++rr) {
             const int r = warp * ROWS + rr;
             const int64_t gi = i0 + r, gg = gi + goff;
-            ract[rr] = col_ok && gi < row_end && has_out && gg >= R && gg < n - R;
+            ract[rr] = out_via_rows && col_ok && gi < row_end && has_out && gg >= R && gg < n - R;
 #pragma unroll
             for (int k = 0; k < CPT; ++k) o[rr][k] = ract[rr] ? load_out(r, k) : 0ull;
         }
@@ -1447,7 +1497,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
             const int r = warp * ROWS + rr;
             const int64_t gi = i0 + r, gg = gi + goff;
             if (!col_ok || gi >= row_end) continue;
-            store_row(r, o[rr], has_out && gg >= R && gg < n - R);
+            store_row(r, o[rr], out_via_rows && has_out && gg >= R && gg < n - R);
         }
     }
 }
@@ -1503,7 +1553,8 @@ __global__ void __launch_bounds__(THREADS, min_blocks<P, R, DT, STEPS, TH_>())
         return;
     }
     process_tile<P, R, DT, STEPS, OUT_SMEM, TH_>(smem, s_red, i0, j0, n, has_out, in_next_v, out_v, true, depth, goff,
-                                                 row_end);
+                                                 row_end,
+                                                 table_route<P, R, DT>() ? smem + table_offset<DT, R, TH_>() : nullptr);
 }
 
 template <int P, int R, int DT, int STEPS, int TH_>

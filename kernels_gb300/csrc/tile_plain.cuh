@@ -15,11 +15,15 @@
 namespace prk {
 namespace plain {
 
-template <int DT, int R>
+// Shared memory: the staged `in` tile, the certification's reduction words, and the product tables of
+// the table route (tile::table_tile) for the stencils that take it.
+template <int P, int DT, int R>
 struct Smem {
     using G = tile::Geo<DT, R>;
     static constexpr int RED_OFF = (G::IN_BYTES + 127) / 128 * 128;
-    static constexpr int BYTES = RED_OFF + tile::WARPS * 8;
+    static constexpr int TBL_OFF = (RED_OFF + tile::WARPS * 8 + 15) / 16 * 16;
+    static constexpr int BYTES = TBL_OFF + tile::table_bytes<P, R, DT>();
+    static_assert(BYTES <= tile::SMEM_PER_CTA_MAX, "the tile and its tables must fit in shared memory");
 };
 
 // Resident CTAs per SM the register budget is cut for: the TMA kernel's, except for the FP64
@@ -43,13 +47,14 @@ __global__ void __launch_bounds__(tile::THREADS, plain_min_blocks<P, R, DT, STEP
 {
     using C = tile::Cfg<DT>;
     extern __shared__ __align__(128) unsigned char smem[];
-    int* s_red = reinterpret_cast<int*>(smem + Smem<DT, R>::RED_OFF);
+    int* s_red = reinterpret_cast<int*>(smem + Smem<P, DT, R>::RED_OFF);
     const int64_t i0 = row0 + static_cast<int64_t>(blockIdx.y) * C::TH;
     const int64_t j0 = static_cast<int64_t>(blockIdx.x) * C::TW;
     const bool has_out = tile::tile_has_out(i0 + goff, j0, n, R, C::TW, C::TH);
     batch::stage_tile<R, DT>(smem, in, n, nr, i0, j0);
-    tile::process_tile<P, R, DT, STEPS, tile::OUT_HBM_AHEAD>(smem, s_red, i0, j0, n, has_out, in_next, out, false, depth,
-                                                             goff, row_end);
+    tile::process_tile<P, R, DT, STEPS, tile::OUT_HBM_AHEAD>(
+        smem, s_red, i0, j0, n, has_out, in_next, out, false, depth, goff, row_end,
+        tile::table_route<P, R, DT>() ? smem + Smem<P, DT, R>::TBL_OFF : nullptr);
 }
 
 // The arguments of one launch: `depth` applications from in into in_next, accumulating into out,
@@ -72,7 +77,7 @@ template <int P, int R, int DT, int STEPS>
 cudaError_t launch(const Args& a)
 {
     using C = tile::Cfg<DT>;
-    constexpr int SM = Smem<DT, R>::BYTES;
+    constexpr int SM = Smem<P, DT, R>::BYTES;
     if (cudaError_t e = cudaFuncSetAttribute(k_stencil_plain<P, R, DT, STEPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM))
         return e;
     const int64_t nr = a.nr > 0 ? a.nr : a.n;
