@@ -11,7 +11,9 @@ int ctas_per_sm_fp64_pow2(int steps) { return ctas_per_sm_depth<FP64, FAM_POW2>(
 
 cudaError_t launch_family(int dtype, int fam, int steps, const Launch& L)
 {
-    if (dtype == FP32C) return fam == FAM_ALL ? launch_fp32c(steps, L) : cudaErrorInvalidValue;
+    if (dtype == FP32C)
+        return fam == FAM_F32_STAR ? launch_fp32c_star(steps, L)
+                                   : (fam == FAM_F32_GRID ? launch_fp32c_grid(steps, L) : cudaErrorInvalidValue);
     switch (fam) {
     case FAM_POW2: return launch_fp64_pow2(steps, L);
     case fam_one(STAR, 3): return launch_fp64_star3(steps, L);
@@ -27,7 +29,8 @@ cudaError_t launch_family(int dtype, int fam, int steps, const Launch& L)
 
 int ctas_per_sm_family(int dtype, int fam, int steps)
 {
-    if (dtype == FP32C) return fam == FAM_ALL ? ctas_per_sm_fp32c(steps) : 0;
+    if (dtype == FP32C)
+        return fam == FAM_F32_STAR ? ctas_per_sm_fp32c_star(steps) : (fam == FAM_F32_GRID ? ctas_per_sm_fp32c_grid(steps) : 0);
     switch (fam) {
     case FAM_POW2: return ctas_per_sm_fp64_pow2(steps);
     case fam_one(STAR, 3): return ctas_per_sm_fp64_star3(steps);

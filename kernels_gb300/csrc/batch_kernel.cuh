@@ -32,16 +32,18 @@ struct GridDesc {
 };
 
 // Kernel families: the stencils one instantiation of the batched kernel evaluates, so that no kernel
-// carries the code and registers of stencils it does not run. FP32C: one family of every stencil.
-// FP64: the power-of-two stencils (star R=1,2 and grid R=1, the certified exact routes), and each
-// stencil with other weights on its own (the table route).
-constexpr int FAM_ALL = 0;
-constexpr int FAM_POW2 = 1;
+// carries the code and registers of stencils it does not run. FP32C: the star stencils, and the grid
+// stencils. FP64: the power-of-two stencils (star R=1,2 and grid R=1, the certified exact routes),
+// and each stencil with other weights on its own (the table route).
+constexpr int FAM_F32_STAR = 0;
+constexpr int FAM_F32_GRID = 1;
+constexpr int FAM_POW2 = 2;
 __host__ __device__ constexpr int fam_one(int P, int R) { return 16 + 8 * P + R; }
 
 __host__ __device__ constexpr bool in_family(int fam, int P, int R, int DT)
 {
-    if (fam == FAM_ALL) return DT == FP32C;
+    if (fam == FAM_F32_STAR) return DT == FP32C && P == STAR;
+    if (fam == FAM_F32_GRID) return DT == FP32C && P == GRID;
     if (fam == FAM_POW2) return DT == FP64 && pow2_weights(P, R);
     return DT == FP64 && fam == fam_one(P, R) && !pow2_weights(P, R);
 }
@@ -49,7 +51,7 @@ __host__ __device__ constexpr bool in_family(int fam, int P, int R, int DT)
 // The family that evaluates a grid of (pattern, R) in storage form dtype.
 __host__ __device__ constexpr int family_of(int dtype, int P, int R)
 {
-    return dtype == FP32C ? FAM_ALL : (pow2_weights(P, R) ? FAM_POW2 : fam_one(P, R));
+    return dtype == FP32C ? (P == STAR ? FAM_F32_STAR : FAM_F32_GRID) : (pow2_weights(P, R) ? FAM_POW2 : fam_one(P, R));
 }
 
 template <int DT, int FAM>
@@ -77,12 +79,14 @@ constexpr int max_table_bytes()
     return m;
 }
 
-// Shared memory: the staged `in` tile, the reduction words, and the table route's product tables.
+// Shared memory: the staged `in` tile, the reduction words, and the table route's product tables
+// followed by its out area (tile::table_tile).
 template <int DT, int FAM>
 struct Layout {
     static constexpr int RED_OFF = (max_in_bytes<DT, FAM>() + 127) / 128 * 128;
     static constexpr int TBL_OFF = (RED_OFF + tile::WARPS * 8 + 15) / 16 * 16;
-    static constexpr int SMEM = TBL_OFF + max_table_bytes<DT, FAM>();
+    static constexpr int SMEM =
+        TBL_OFF + max_table_bytes<DT, FAM>() + (max_table_bytes<DT, FAM>() > 0 ? tile::table_out_bytes() : 0);
     static_assert(SMEM <= tile::SMEM_PER_CTA_MAX, "the tile and its tables must fit in shared memory");
 };
 
@@ -138,9 +142,13 @@ __device__ __forceinline__ void item(unsigned char* smem, int* s_red, const Grid
     const int64_t n = g.n;
     const int64_t i0 = (t / g.tiles_x) * C::TH;
     const int64_t j0 = (t % g.tiles_x) * C::TW;
-    stage_tile<R, DT>(smem, g.in[parity], n, n, i0, j0);
+    // the two in buffers picked without indexing g.in by a run-time value (which would put g in
+    // local memory)
+    void* const in_cur = parity ? g.in[1] : g.in[0];
+    void* const in_nxt = parity ? g.in[0] : g.in[1];
+    stage_tile<R, DT>(smem, in_cur, n, n, i0, j0);
     tile::process_tile<P, R, DT, STEPS, tile::OUT_HBM>(smem, s_red, i0, j0, n, tile::tile_has_out(i0, j0, n, R, C::TW, C::TH),
-                                               g.in[parity ^ 1], g.out, g.vec_ok != 0, depth, 0, n,
+                                               in_nxt, g.out, g.vec_ok != 0, depth, 0, n,
                                                tile::table_route<P, R, DT>() ? tbl : nullptr);
 }
 
@@ -247,8 +255,8 @@ int ctas_per_sm_depth(int steps)
 }
 
 // Per-family entry points, one translation unit each so that the build compiles them in parallel:
-// batch_fp64_pow2.cu, batch_fp64_strict_*.cu (one per stencil with other weights) and the FP32C
-// depths (batch_fp32c.cu with batch_fp32c_deep.cu).
+// batch_fp64_pow2.cu, batch_fp64_strict_*.cu (one per stencil with other weights),
+// batch_fp32c_star.cu and batch_fp32c_grid.cu.
 cudaError_t launch_fp64_pow2(int steps, const Launch& L);
 int ctas_per_sm_fp64_pow2(int steps);
 #define PRK_BATCH_STRICT_DECL(PN, RR)                                 \
@@ -263,17 +271,10 @@ PRK_BATCH_STRICT_DECL(grid, 4)
 PRK_BATCH_STRICT_DECL(grid, 5)
 #undef PRK_BATCH_STRICT_DECL
 
-// The FP32C depths are instantiated in two translation units; the dispatching unit declares the
-// other's with this.
-#define PRK_BATCH_EXTERN(DT, S, F)                                  \
-    extern template cudaError_t launch<DT, S, F>(const Launch& L); \
-    extern template int ctas_per_sm<DT, S, F>();
-#define PRK_BATCH_INSTANTIATE(DT, S, F)                      \
-    template cudaError_t launch<DT, S, F>(const Launch& L); \
-    template int ctas_per_sm<DT, S, F>();
-
-cudaError_t launch_fp32c(int steps, const Launch& L);
-int ctas_per_sm_fp32c(int steps);
+cudaError_t launch_fp32c_star(int steps, const Launch& L);
+int ctas_per_sm_fp32c_star(int steps);
+cudaError_t launch_fp32c_grid(int steps, const Launch& L);
+int ctas_per_sm_fp32c_grid(int steps);
 
 // Dispatch by family (host side): a grid's family as family_of gives it.
 cudaError_t launch_family(int dtype, int fam, int steps, const Launch& L);

@@ -901,15 +901,21 @@ __device__ __forceinline__ void table_chain(const int32_t* sp, const uint64_t* T
     }
 }
 
+// Bytes of the shared-memory out area the table route needs besides its tables in kernels that keep
+// out in HBM (one FP64 tile of out words; the TMA kernel updates its out tile instead).
+__host__ __device__ constexpr int table_out_bytes() { return Cfg<FP64>::TW * Cfg<FP64>::TH * 8; }
+
 // The table route for a whole tile whose int32 values (the tile's in, halo included) lie in
 // [lo, hi]: `nsteps` applications, with the int32 tile advanced in place between them, as the other
-// routes leave it for the stores. Lane l owns columns l and l + 32 of its warp's rows; their out
-// words stay in registers across the applications, read from and written back to the shared-memory
-// out tile (OUT_SMEM) or the out array itself (the other sources: out_g points at the tile's (0, 0),
-// row stride n). Returns false, having done nothing, when the values span TBL_L or more (lo and hi
-// are block-uniform).
+// routes leave it for the stores. Lane l owns columns l and l + 32 of its warp's rows; every
+// application adds its S into their out words in o_s, a shared-memory tile of out words (row stride
+// TW). With OUT_SMEM, o_s is the TMA kernel's out tile, which the stores then read in their own
+// layout; with the other sources o_s is scratch, filled from the out array (out_g points at the
+// tile's (0, 0), row stride n) before the first application and written back after the last, each
+// thread its own points. Returns false, having done nothing, when the values span TBL_L or more (lo
+// and hi are block-uniform).
 template <int P, int R, int SW, int SH, int TW, int ROWS, int OUT_SRC>
-__device__ __forceinline__ bool table_tile(int32_t* si, uint64_t* o_tile, uint64_t* out_g, unsigned char* tbl, int lo,
+__device__ __forceinline__ bool table_tile(int32_t* si, uint64_t* o_s, uint64_t* out_g, unsigned char* tbl, int lo,
                                            int hi, int nsteps, int64_t i0, int64_t j0, int64_t n, int64_t goff,
                                            int64_t row_end, bool has_out)
 {
@@ -921,21 +927,17 @@ __device__ __forceinline__ bool table_tile(int32_t* si, uint64_t* o_tile, uint64
     uint4* T96 = reinterpret_cast<uint4*>(tbl + group_count<P, R>() * TBL_L * 8);
     int base = lo;
     build_tables<P, R>(T64, T96, base);
-    // the thread's out words
-    uint64_t o[ROWS][2];
+    if constexpr (OUT_SRC != OUT_SMEM) {
 #pragma unroll
-    for (int rr = 0; rr < ROWS; ++rr) {
-        const int r = warp * ROWS + rr;
-        const int64_t gi = i0 + r;
-        const bool act = table_row_active(has_out, gi, gi + goff, row_end, n, R);
+        for (int rr = 0; rr < ROWS; ++rr) {
+            const int r = warp * ROWS + rr;
+            const int64_t gi = i0 + r;
+            if (!table_row_active(has_out, gi, gi + goff, row_end, n, R)) continue;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int c = lane + 32 * h;
-            const bool col = j0 + c >= R && j0 + c < n - R;
-            if constexpr (OUT_SRC == OUT_SMEM)
-                o[rr][h] = act ? o_tile[r * TW + c] : 0ull;
-            else
-                o[rr][h] = act && col ? out_g[r * n + c] : 0ull;
+            for (int h = 0; h < 2; ++h) {
+                const int c = lane + 32 * h;
+                if (j0 + c >= R && j0 + c < n - R) o_s[r * TW + c] = out_g[r * n + c];
+            }
         }
     }
     __syncthreads();  // the tables complete
@@ -958,23 +960,24 @@ __device__ __forceinline__ bool table_tile(int32_t* si, uint64_t* o_tile, uint64
             double d[2];
             table_chain<P, R, SW>(s0 + r * SW + lane, T64, T96, base, d);
 #pragma unroll
-            for (int h = 0; h < 2; ++h) o[rr][h] = as_bits(__dadd_rn(as_dbl(o[rr][h]), d[h]));
+            for (int h = 0; h < 2; ++h) {
+                const int c = lane + 32 * h;
+                if (j0 + c >= R && j0 + c < n - R)
+                    o_s[r * TW + c] = as_bits(__dadd_rn(as_dbl(o_s[r * TW + c]), d[h]));
+            }
         }
         if (t + 1 < nsteps) __syncthreads();  // every thread's reads done before the next advance
     }
+    if constexpr (OUT_SRC != OUT_SMEM) {
 #pragma unroll
-    for (int rr = 0; rr < ROWS; ++rr) {
-        const int r = warp * ROWS + rr;
-        const int64_t gi = i0 + r;
-        if (!table_row_active(has_out, gi, gi + goff, row_end, n, R)) continue;
+        for (int rr = 0; rr < ROWS; ++rr) {
+            const int r = warp * ROWS + rr;
+            const int64_t gi = i0 + r;
+            if (!table_row_active(has_out, gi, gi + goff, row_end, n, R)) continue;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int c = lane + 32 * h;
-            if (j0 + c >= R && j0 + c < n - R) {
-                if constexpr (OUT_SRC == OUT_SMEM)
-                    o_tile[r * TW + c] = o[rr][h];
-                else
-                    out_g[r * n + c] = o[rr][h];
+            for (int h = 0; h < 2; ++h) {
+                const int c = lane + 32 * h;
+                if (j0 + c >= R && j0 + c < n - R) out_g[r * n + c] = o_s[r * TW + c];
             }
         }
     }
@@ -1164,8 +1167,10 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
                 lo = min(lo, s_red[2 * w]);
                 hi = max(hi, s_red[2 * w + 1]);
             }
+            // kernels that keep out in HBM give the route an out area right after the tables
+            uint64_t* o_s = OUT_SRC == OUT_SMEM ? o_tile : reinterpret_cast<uint64_t*>(tbl + table_bytes<P, R, DT>());
             tbl_done = table_tile<P, R, G::SW, G::SH, C::TW, ROWS, OUT_SRC>(
-                reinterpret_cast<int32_t*>(s_in), o_tile, static_cast<uint64_t*>(out_v) + i0 * n + j0, tbl, lo, hi,
+                reinterpret_cast<int32_t*>(s_in), o_s, static_cast<uint64_t*>(out_v) + i0 * n + j0, tbl, lo, hi,
                 nsteps, i0, j0, n, goff, row_end, has_out);
         }
     }

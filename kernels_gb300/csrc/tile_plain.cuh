@@ -15,14 +15,15 @@
 namespace prk {
 namespace plain {
 
-// Shared memory: the staged `in` tile, the certification's reduction words, and the product tables of
-// the table route (tile::table_tile) for the stencils that take it.
+// Shared memory: the staged `in` tile, the certification's reduction words, and for the stencils that
+// take the table route (tile::table_tile) its product tables followed by its out area.
 template <int P, int DT, int R>
 struct Smem {
     using G = tile::Geo<DT, R>;
     static constexpr int RED_OFF = (G::IN_BYTES + 127) / 128 * 128;
     static constexpr int TBL_OFF = (RED_OFF + tile::WARPS * 8 + 15) / 16 * 16;
-    static constexpr int BYTES = TBL_OFF + tile::table_bytes<P, R, DT>();
+    static constexpr int BYTES =
+        TBL_OFF + tile::table_bytes<P, R, DT>() + (tile::table_route<P, R, DT>() ? tile::table_out_bytes() : 0);
     static_assert(BYTES <= tile::SMEM_PER_CTA_MAX, "the tile and its tables must fit in shared memory");
 };
 

@@ -55,10 +55,12 @@ def test_mixed_batch_fp64_bit_exact(cuda, depth, graph):
 
 @pytest.mark.parametrize("graph", [False, True])
 def test_mixed_batch_whole_run_fp64_bit_exact(cuda, graph):
-    """Every grid's timed applications in one launch of the batched kernel."""
+    """Every grid's timed applications in one launch of the batched kernel per kernel family (the
+    power-of-two stencils share one; every stencil with other weights has its own)."""
     k = 9
     b, grids = make_batch(cuda, VALID, kg.FP64, whole=True)
-    assert b.launches(k) == 1
+    families = {"pow2" if (p, r) in ((kg.STAR, 1), (kg.STAR, 2), (kg.GRID, 1)) else (p, r) for p, r, _ in VALID}
+    assert b.launches(k) == len(families)
     b.run(k, graph=graph)
     check_fp64(b, grids, VALID, k)
     assert all(abs(x - 2.0 * (k + 1)) <= 1e-8 for x in b.norms())
