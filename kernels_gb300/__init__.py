@@ -32,7 +32,7 @@ FP64, FP32C = 0, 1
 RUN_GRAPH, RUN_UNFUSED, RUN_TUNED, RUN_TALL, RUN_WHOLE = 1, 2, 4, 8, 16
 
 __all__ = ["STAR", "GRID", "FP64", "FP32C", "PrkError", "apply", "add", "init", "norm", "run", "run_host",
-           "alloc", "apply_steps", "flops", "probe_dadd", "slab_run", "slab_norm", "tune", "Batch", "pattern_of", "dtype_of", "version", "set_kernel", "status", "KERNEL_AUTO",
+           "alloc", "apply_steps", "flops", "probe_dadd", "route_split", "slab_run", "slab_norm", "tune", "Batch", "pattern_of", "dtype_of", "version", "set_kernel", "status", "KERNEL_AUTO",
            "KERNEL_GENERIC", "KERNEL_TMA"] + \
           [f"{p}{r}" for p in ("star", "grid") for r in range(1, 6)]
 
@@ -99,6 +99,14 @@ def probe_dadd() -> float:
     res = C.c_double()
     check(load().prk_gb300_probe_dadd(C.byref(res)))
     return res.value
+
+
+def route_split(pattern: int, radius: int) -> tuple[int, int] | None:
+    """(fixed-point adds, binary64 adds) per interior point and application of the FP64 table route
+    (prk_gb300_route_split), or None for the power-of-two stencils, which take the exact routes."""
+    f, d = C.c_int(), C.c_int()
+    rc = load().prk_gb300_route_split(pattern, radius, C.byref(f), C.byref(d))
+    return None if rc != 0 else (f.value, d.value)
 
 
 def flops(pattern: int, radius: int, n: int) -> float:

@@ -56,13 +56,12 @@ def launches_per_run(iterations: int, depth: int) -> int:
 
 
 def binary64_adds_per_point(pattern: int, r: int) -> int:
-    """Rounded binary64 adds one application needs per interior point in the strict order: the
-    chain's tap_count - 1 adds plus the add into out (the products come from the integer pipes on
-    whole-number tiles). The power-of-two stencils (star R=1,2 and grid R=1) need none on the
-    certified route, where the sum is exact."""
-    if (pattern == kg.STAR and r <= 2) or (pattern == kg.GRID and r == 1):
-        return 0
-    return 4 * r if pattern == kg.STAR else 4 * r * r + 2 * r
+    """Rounded binary64 adds one FP64 application issues per interior point on whole-number tiles: for
+    the stencils whose weights are not powers of two, the part of the reference's chain the table
+    route leaves on the binary64 pipe plus the add into out (prk_gb300_route_split); the power-of-two
+    stencils need none on the certified routes, where the sum is exact."""
+    split = kg.route_split(pattern, r)
+    return 0 if split is None else split[1]
 
 
 def one_case(torch, pattern: int, r: int, n: int, iterations: int, dtype: int, pts, depth: int | None = None):
@@ -115,7 +114,8 @@ def one_case(torch, pattern: int, r: int, n: int, iterations: int, dtype: int, p
         rate = dadd_rate()
         t_adds = adds * (n - 2 * r) ** 2 / rate
         rec["roofline"]["binary64_add_ceiling"] = {
-            "adds_per_point": adds, "measured_adds_per_s": round(rate, 1),
+            "adds_per_point": adds, "fixed_point_adds_per_point": kg.route_split(pattern, r)[0],
+            "measured_adds_per_s": round(rate, 1),
             "ms_per_application": round(t_adds * 1e3, 4), "frac": round(t_adds / per_app, 4)}
     del in_a, in_b, out, res
     torch.cuda.empty_cache()

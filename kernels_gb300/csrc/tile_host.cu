@@ -82,6 +82,25 @@ bool tma_eligible(const StencilCall& c)
 
 bool tma_depth_ok(int steps) { return steps == 1 || steps == 2 || steps == 4 || steps == 8; }
 
+int table_route_split(int pattern, int R, int* fixed_adds, int* binary64_adds)
+{
+    int kf = -1, n = 0;
+#define PRK_SPLIT(PP, RR)                                              \
+    if (pattern == PP && R == RR) {                                    \
+        if constexpr (tile::table_route<PP, RR, FP64>()) {              \
+            kf = tile::fixed_taps<PP, RR>();                            \
+            n = tap_count(PP, RR);                                      \
+        }                                                               \
+    }
+    PRK_SPLIT(STAR, 1) PRK_SPLIT(STAR, 2) PRK_SPLIT(STAR, 3) PRK_SPLIT(STAR, 4) PRK_SPLIT(STAR, 5)
+    PRK_SPLIT(GRID, 1) PRK_SPLIT(GRID, 2) PRK_SPLIT(GRID, 3) PRK_SPLIT(GRID, 4) PRK_SPLIT(GRID, 5)
+#undef PRK_SPLIT
+    if (kf < 0) return -1;
+    *fixed_adds = kf - 1;       // the fixed prefix starts from its first product
+    *binary64_adds = n - kf + 1;  // the rest of the chain, and the add into out
+    return 0;
+}
+
 bool tma_rows_ok(int tile_rows) { return tile_rows == tile::TH_DEFAULT || tile_rows == tile::TH_TALL; }
 
 namespace {
