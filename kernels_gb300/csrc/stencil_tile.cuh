@@ -1507,6 +1507,13 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
     }
 }
 
+#ifndef PRK_STRICT_BLOCKS_1
+#define PRK_STRICT_BLOCKS_1 3
+#endif
+#ifndef PRK_STRICT_BLOCKS_N
+#define PRK_STRICT_BLOCKS_N 3
+#endif
+
 // Register budget: the single-application kernels keep as many tiles resident as shared memory
 // allows, so that every SM has enough loads in flight; the multi-application kernels hold `out` in
 // registers and run at most four tiles per SM. The strict FP64 form is bound by the binary64 pipe
@@ -1514,7 +1521,9 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
 template <int P, int R, int DT, int STEPS, int TH_>
 constexpr int min_blocks()
 {
-    if (DT == FP64 && !pow2_weights(P, R)) return STEPS == 1 ? 2 : 1;
+    // the table route: three tiles per SM (80 registers), so that 24 warps hide the fixed-point
+    // chains' latencies (at four, 64 registers, the longer chains spill)
+    if (DT == FP64 && !pow2_weights(P, R)) return STEPS == 1 ? PRK_STRICT_BLOCKS_1 : PRK_STRICT_BLOCKS_N;
     if (DT == FP32C && P == GRID && R >= 3) return 2;  // bound by FP32 issue: registers over residency
     const int b = Geo<DT, R, TH_>::CTAS;
     if (STEPS == 1) return b;

@@ -34,6 +34,9 @@ struct Smem {
 template <int P, int R, int DT, int STEPS>
 constexpr int plain_min_blocks()
 {
+    // the stencils with other weights carry both the table route and the product route here: the
+    // registers of two tiles per SM for one application, and of one for several, avoid spilling
+    if (tile::table_route<P, R, DT>()) return STEPS == 1 ? 2 : 1;
     constexpr int b = tile::min_blocks<P, R, DT, STEPS, tile::TH_DEFAULT>();
     return DT == FP64 && pow2_weights(P, R) && STEPS == 1 && b > 5 ? 5 : b;
 }
