@@ -1031,6 +1031,24 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
             return o_tile[r * C::TW + c0 + k];
         }
     };
+    // the CPT out words of row r: from HBM as 16-byte vectors where the row's words start on a 16-byte
+    // boundary and lie inside the grid (every other row when n is odd), else one by one
+    auto load_out_row = [&](int r, uint64_t (&o)[CPT]) {
+        if constexpr (OUT_SRC != OUT_SMEM) {
+            const uint64_t* src = static_cast<const uint64_t*>(out_v) + (i0 + r) * n + gj;
+            if (gj + CPT <= n && (reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
+#pragma unroll
+                for (int k = 0; k < CPT; k += 2) {
+                    const ulonglong2 w = *reinterpret_cast<const ulonglong2*>(src + k);
+                    o[k] = w.x;
+                    o[k + 1] = w.y;
+                }
+                return;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < CPT; ++k) o[k] = load_out(r, k);
+    };
 
     // ---- FP64 power-of-two stencils: certify the tile for an exact route ----
     // First the FP32 route: every value +0 or an integer of magnitude below 2^20 (checked with a few
@@ -1298,7 +1316,9 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
             }
         }
         T* nx = static_cast<T*>(in_next_v) + gi * n + gj;
-        if (vec_ok) {
+        // 16-byte stores wherever the row's words start on a 16-byte boundary inside the grid (every
+        // row for the TMA tiles; every other row for an odd n)
+        if (vec_ok || (gj + CPT <= n && (reinterpret_cast<uintptr_t>(nx) & 15u) == 0)) {
             st_vec(nx, nxt);
         } else {
 #pragma unroll
@@ -1307,7 +1327,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
         }
         if (row_out) {
             uint64_t* out = static_cast<uint64_t*>(out_v) + gi * n + gj;
-            if (vec_ok && cols_interior) {
+            if (cols_interior && (vec_ok || (reinterpret_cast<uintptr_t>(out) & 15u) == 0)) {
 #pragma unroll
                 for (int k = 0; k < CPT; k += 2) *reinterpret_cast<ulonglong2*>(out + k) = make_ulonglong2(o[k], o[k + 1]);
             } else {
@@ -1330,8 +1350,12 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
                 const int r = warp * ROWS + rr;
                 const int64_t gi = i0 + r, gg = gi + goff;
                 const bool row_out = col_ok && gi < row_end && has_out && gg >= R && gg < n - R;
+                if (row_out) {
+                    load_out_row(r, o_pre[rr]);
+                } else {
 #pragma unroll
-                for (int k = 0; k < CPT; ++k) o_pre[rr][k] = row_out ? load_out(r, k) : 0ull;
+                    for (int k = 0; k < CPT; ++k) o_pre[rr][k] = 0ull;
+                }
             }
         }
 #pragma unroll
@@ -1342,12 +1366,11 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
             const bool row_out = out_via_rows && has_out && gg >= R && gg < n - R;
             uint64_t o[CPT];
             if (row_out) {
+                if constexpr (PRELOAD) {
 #pragma unroll
-                for (int k = 0; k < CPT; ++k) {
-                    if constexpr (PRELOAD)
-                        o[k] = o_pre[rr][k];
-                    else
-                        o[k] = load_out(r, k);
+                    for (int k = 0; k < CPT; ++k) o[k] = o_pre[rr][k];
+                } else {
+                    load_out_row(r, o);
                 }
                 if (!tbl_done) apply_row(r, o);
             }
@@ -1363,8 +1386,12 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
             const int r = warp * ROWS + rr;
             const int64_t gi = i0 + r, gg = gi + goff;
             ract[rr] = out_via_rows && col_ok && gi < row_end && has_out && gg >= R && gg < n - R;
+            if (ract[rr]) {
+                load_out_row(r, o[rr]);
+            } else {
 #pragma unroll
-            for (int k = 0; k < CPT; ++k) o[rr][k] = ract[rr] ? load_out(r, k) : 0ull;
+                for (int k = 0; k < CPT; ++k) o[rr][k] = 0ull;
+            }
         }
         if constexpr (EXACT) {
             // FP32 route: when every out word the tile stores is an integer V of 2^-SHIFT units with
