@@ -33,6 +33,22 @@ def test_version_and_pure_functions():
     assert kg.flops(kg.GRID, 5, 1000) == (2 * 121 + 1) * 990.0 ** 2
 
 
+def test_route_split_covers_every_add_of_the_chain():
+    """prk_gb300_route_split: for the stencils whose weights are not powers of two, the fixed-point
+    and binary64 adds of one application per point are the chain's taps - 1 adds plus the add into
+    out; most of each chain runs in fixed point. The power-of-two stencils are rejected (they take the
+    exact routes)."""
+    for p, r in [(kg.STAR, 3), (kg.STAR, 4), (kg.STAR, 5), (kg.GRID, 2), (kg.GRID, 3), (kg.GRID, 4), (kg.GRID, 5)]:
+        taps = 4 * r if p == kg.STAR else 4 * r * r + 2 * r
+        fixed, dp = kg.route_split(p, r)
+        assert fixed + dp == taps, (p, r)
+        assert taps // 2 <= fixed < taps and dp >= 2
+    for p, r in [(kg.STAR, 1), (kg.STAR, 2), (kg.GRID, 1)]:
+        assert kg.route_split(p, r) is None
+    f, d = C.c_int(), C.c_int()
+    assert _lib.load().prk_gb300_route_split(kg.STAR, 6, C.byref(f), C.byref(d)) == -1
+
+
 @pytest.mark.parametrize("args,code", [
     ((kg.STAR, 0, 100, kg.FP64), -1),     # radius < 1
     ((kg.STAR, 6, 100, kg.FP64), -1),     # radius > 5

@@ -79,3 +79,11 @@ def test_prk_field_norm_n16384(cuda):
     kg.init(in_a, out)
     kg.apply(kg.STAR, r, in_a, out, in_next=in_b)
     assert abs(kg.norm(r, out) - 2.0) <= 1e-8
+
+
+def test_dadd_probe_measures_a_plausible_rate(cuda):
+    """The binary64 add rate the bench and the sweep divide by: positive and below the SM count
+    times a generous 4 adds per SM per clock at 2.5 GHz."""
+    rate = kg.probe_dadd()
+    sms = cuda.cuda.get_device_properties(0).multi_processor_count
+    assert 1e10 < rate < sms * 4 * 2.5e9
