@@ -905,22 +905,44 @@ __device__ __forceinline__ void table_chain(const int32_t* sp, const uint64_t* T
 // out in HBM (one FP64 tile of out words; the TMA kernel updates its out tile instead).
 __host__ __device__ constexpr int table_out_bytes() { return Cfg<FP64>::TW * Cfg<FP64>::TH * 8; }
 
+// dst = src + 1 over a whole int32 tile, halo included, as 16-byte vectors.
+template <int ELEMS>
+__device__ __forceinline__ void advance_i32_to(const int32_t* src, int32_t* dst)
+{
+    constexpr int NV = ELEMS / 4;
+#pragma unroll
+    for (int q = 0; q < (NV + THREADS - 1) / THREADS; ++q) {
+        const int idx = threadIdx.x + q * THREADS;
+        if (NV % THREADS == 0 || idx < NV) {
+            int4 v = reinterpret_cast<const int4*>(src)[idx];
+            v.x += 1;
+            v.y += 1;
+            v.z += 1;
+            v.w += 1;
+            reinterpret_cast<int4*>(dst)[idx] = v;
+        }
+    }
+}
+
 // The table route for a whole tile whose int32 values (the tile's in, halo included) lie in
-// [lo, hi]: `nsteps` applications, with the int32 tile advanced in place between them, as the other
-// routes leave it for the stores. Lane l owns columns l and l + 32 of its warp's rows; every
-// application adds its S into their out words in o_s, a shared-memory tile of out words (row stride
-// TW). With OUT_SMEM, o_s is the TMA kernel's out tile, which the stores then read in their own
-// layout; with the other sources o_s is scratch, filled from the out array (out_g points at the
-// tile's (0, 0), row stride n) before the first application and written back after the last, each
-// thread its own points. Returns false, having done nothing, when the values span TBL_L or more (lo
-// and hi are block-uniform).
+// [lo, hi]: `nsteps` applications. The int32 tile takes half of the FP64 stage, so the other half
+// holds the next application's in: while application t reads one, in + 1 goes to the other, and
+// one barrier per application separates them; *fin (0 or SW * SH) is where the last application's
+// in is left for the stores. Lane l owns columns l and l + 32 of its warp's rows; every application
+// adds its S into their out words in o_s, a shared-memory tile of out words (row stride TW). With
+// OUT_SMEM, o_s is the TMA kernel's out tile, which the stores then read in their own layout; with
+// the other sources o_s is scratch, filled from the out array (out_g points at the tile's (0, 0),
+// row stride n) before the first application and written back after the last, each thread its own
+// points. Returns false, having done nothing, when the values span TBL_L or more (lo and hi are
+// block-uniform).
 template <int P, int R, int SW, int SH, int TW, int ROWS, int OUT_SRC>
 __device__ __forceinline__ bool table_tile(int32_t* si, uint64_t* o_s, uint64_t* out_g, unsigned char* tbl, int lo,
                                            int hi, int nsteps, int64_t i0, int64_t j0, int64_t n, int64_t goff,
-                                           int64_t row_end, bool has_out)
+                                           int64_t row_end, bool has_out, int* fin)
 {
     constexpr int ELEMS = SW * SH;
     static_assert(TW == 64, "two columns per lane, 32 apart");
+    static_assert(ELEMS % 4 == 0, "the advance moves 16-byte vectors");
     if (hi - lo >= TBL_L) return false;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint64_t* T64 = reinterpret_cast<uint64_t*>(tbl);
@@ -941,17 +963,15 @@ __device__ __forceinline__ bool table_tile(int32_t* si, uint64_t* o_s, uint64_t*
         }
     }
     __syncthreads();  // the tables complete
-    const int32_t* s0 = si + R * SW + ((SW - TW) / 2);  // the tile's (0, 0)
+    int cur = 0;
 #pragma unroll 1
     for (int t = 0; t < nsteps; ++t) {
-        if (t > 0) {
-            advance_i32<ELEMS>(si);
-            if (hi + t >= base + TBL_L) {  // the values outgrew the table: rebuild it at the new minimum
-                base = lo + t;
-                build_tables<P, R>(T64, T96, base);
-            }
+        if (t > 0 && hi + t >= base + TBL_L) {  // the values outgrew the table: rebuild it at the new minimum
+            base = lo + t;
+            build_tables<P, R>(T64, T96, base);
             __syncthreads();
         }
+        const int32_t* s0 = si + cur + R * SW + ((SW - TW) / 2);  // the tile's (0, 0)
 #pragma unroll 1
         for (int rr = 0; rr < ROWS; ++rr) {
             const int r = warp * ROWS + rr;
@@ -966,8 +986,13 @@ __device__ __forceinline__ bool table_tile(int32_t* si, uint64_t* o_s, uint64_t*
                     o_s[r * TW + c] = as_bits(__dadd_rn(as_dbl(o_s[r * TW + c]), d[h]));
             }
         }
-        if (t + 1 < nsteps) __syncthreads();  // every thread's reads done before the next advance
+        if (t + 1 < nsteps) {
+            advance_i32_to<ELEMS>(si + cur, si + (ELEMS - cur));
+            cur = ELEMS - cur;
+            __syncthreads();  // the next application's in complete, this one's reads done
+        }
     }
+    *fin = cur;
     if constexpr (OUT_SRC != OUT_SMEM) {
 #pragma unroll
         for (int rr = 0; rr < ROWS; ++rr) {
@@ -1177,6 +1202,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
     // ---- FP64, other weights: the table route (table_tile), when the kernel has a table area and
     // the tile's range fits it ----
     bool tbl_done = false;
+    int iw_fin = 0;  // where the int32 tile of the last application's in lies (int32 elements)
     if constexpr (table_route<P, R, DT>()) {
         if (iwhole && tbl) {
             int lo = s_red[0], hi = s_red[1];
@@ -1189,7 +1215,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
             uint64_t* o_s = OUT_SRC == OUT_SMEM ? o_tile : reinterpret_cast<uint64_t*>(tbl + table_bytes<P, R, DT>());
             tbl_done = table_tile<P, R, G::SW, G::SH, C::TW, ROWS, OUT_SRC>(
                 reinterpret_cast<int32_t*>(s_in), o_s, static_cast<uint64_t*>(out_v) + i0 * n + j0, tbl, lo, hi,
-                nsteps, i0, j0, n, goff, row_end, has_out);
+                nsteps, i0, j0, n, goff, row_end, has_out, &iw_fin);
         }
     }
 
@@ -1300,7 +1326,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
         }
         if constexpr (DT == FP64 && !EXACT) {
             if (iwhole) {
-                const int32_t* v = reinterpret_cast<const int32_t*>(s_in) + soff;
+                const int32_t* v = reinterpret_cast<const int32_t*>(s_in) + iw_fin + soff;
 #pragma unroll
                 for (int k = 0; k < CPT; ++k) nxt[k] = as_dbl(from_fixed32(v[k] + 1, 0));
                 done = true;
