@@ -27,16 +27,14 @@ struct Smem {
     static_assert(BYTES <= tile::SMEM_PER_CTA_MAX, "the tile and its tables must fit in shared memory");
 };
 
-// Resident CTAs per SM the register budget is cut for: the TMA kernel's, except for the FP64
-// power-of-two stencils at one application, whose out words are all requested ahead
-// (tile::OUT_HBM_AHEAD) and which hold them in the registers of five CTAs per SM rather than
-// spilling at six (n=16383, star R=2: 3585 GFLOP/s against 3449 without the early requests).
+// Resident CTAs per SM the register budget is cut for: the TMA kernel's (three tiles per SM for the
+// table route), except for the FP64 power-of-two stencils at one application, whose out words are
+// all requested ahead (tile::OUT_HBM_AHEAD) and which hold them in the registers of five CTAs per SM
+// rather than spilling at six (n=16383, star R=2: 3585 GFLOP/s against 3449 without the early
+// requests).
 template <int P, int R, int DT, int STEPS>
 constexpr int plain_min_blocks()
 {
-    // the stencils with other weights carry both the table route and the product route here: the
-    // registers of two tiles per SM for one application, and of one for several, avoid spilling
-    if (tile::table_route<P, R, DT>()) return STEPS == 1 ? 2 : 1;
     constexpr int b = tile::min_blocks<P, R, DT, STEPS, tile::TH_DEFAULT>();
     return DT == FP64 && pow2_weights(P, R) && STEPS == 1 && b > 5 ? 5 : b;
 }
