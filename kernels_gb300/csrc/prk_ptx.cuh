@@ -1,5 +1,6 @@
-// Inline-PTX wrappers for the Blackwell data movers the stencil kernels use: mbarriers and TMA
-// (cp.async.bulk.tensor) tile loads into shared memory. Every wait is bounded: after the limit it
+// Inline-PTX wrappers for the data movers the stencil kernels use: mbarriers and TMA
+// (cp.async.bulk.tensor) tile loads into shared memory, and per-thread asynchronous copies
+// (cp.async). Every wait is bounded: after the limit it
 // reports failure to the caller instead of spinning forever.
 #pragma once
 
@@ -63,6 +64,22 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
             smem_addr(dst)),
         "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
         : "memory");
+}
+
+// Asynchronous copy (cp.async) of E bytes (4, 8 or 16) from global src to shared dst, both aligned
+// to E; src_bytes = 0 writes E zero bytes without reading src. Completes with cp_async_wait_all.
+template <int E>
+__device__ __forceinline__ void cp_async(void* dst, const void* src, uint32_t src_bytes)
+{
+    static_assert(E == 4 || E == 8 || E == 16, "cp.async sizes");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(smem_addr(dst)), "l"(src), "n"(E), "r"(src_bytes)
+                 : "memory");
+}
+
+// Wait for every cp.async this thread issued.
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
 
 }  // namespace prk

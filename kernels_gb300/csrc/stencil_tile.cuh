@@ -676,35 +676,6 @@ __device__ __forceinline__ void fp64_points_whole(const int32_t* s, double (&acc
     }
 }
 
-// fp64_point for CPT adjacent points with the taps from constant memory in a loop, for the long
-// chains (grid R >= 3) in the plain-staged kernel, where the fully unrolled form has the compiler
-// hoist every tap's load and spill (576 bytes for grid R = 5 at three tiles per SM; the TMA and
-// batched kernels do not spill and keep it): the same products (the weight rebuilt from its split
-// encoding, exactly) and the same sums in the same order, the first product taken as it is (a -0
-// product stays -0).
-template <int P, int R, int LD, int CPT>
-__device__ __forceinline__ void fp64_points_strict(const double* s, double (&acc)[CPT])
-{
-    constexpr int N = tap_count(P, R);
-    const auto& T = c_taps<P, R, LD>;
-    auto wt = [](const typename TapTable<P, R, LD>::Tap& tp) {
-        return __longlong_as_double(static_cast<long long>((static_cast<uint64_t>(tp.hib | (tp.w2 & 0xFFFFFu)) << 32) | tp.w1));
-    };
-    {
-        const auto tp = T.tap[0];
-        const double w = wt(tp);
-#pragma unroll
-        for (int k = 0; k < CPT; ++k) acc[k] = __dmul_rn(s[tp.off + k], w);
-    }
-#pragma unroll 2
-    for (int t = 1; t < N; ++t) {
-        const auto tp = T.tap[t];
-        const double w = wt(tp);
-#pragma unroll
-        for (int k = 0; k < CPT; ++k) acc[k] = __dadd_rn(acc[k], __dmul_rn(s[tp.off + k], w));
-    }
-}
-
 // in += 1 over a staged tile of int32 whole numbers, as 16-byte vectors.
 template <int ELEMS>
 __device__ __forceinline__ void advance_i32(int32_t* p)
@@ -1309,15 +1280,8 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
             }
             if (!done) {
                 const double* sp = reinterpret_cast<const double*>(s_in) + soff;
-                if constexpr (tap_count(P, R) > 24 && OUT_SRC == OUT_HBM_AHEAD) {  // the plain-staged kernel
-                    double S[CPT];
-                    fp64_points_strict<P, R, G::SW, CPT>(sp, S);
 #pragma unroll
-                    for (int k = 0; k < CPT; ++k) o[k] = as_bits(__dadd_rn(as_dbl(o[k]), S[k]));
-                } else {
-#pragma unroll
-                    for (int k = 0; k < CPT; ++k) o[k] = as_bits(__dadd_rn(as_dbl(o[k]), fp64_point<P, R>(sp + k, G::SW)));
-                }
+                for (int k = 0; k < CPT; ++k) o[k] = as_bits(__dadd_rn(as_dbl(o[k]), fp64_point<P, R>(sp + k, G::SW)));
             }
         } else {
             const float* sp = reinterpret_cast<const float*>(s_in) + soff;
