@@ -339,7 +339,7 @@ def run_gb300(args) -> None:
         # the reference's chain rounds every one of its adds: on whole-number tiles the table route
         # runs the first part of each chain in exact fixed point on the integer pipes and the rest,
         # with the add into out, on the binary64 pipe
-        fixed_adds, dp_adds = kg.route_split(kg.GRID, r)
+        fixed_adds, dp_adds = kg.route_split(kg.GRID, r, 1)  # one application per launch
         pts = (n - 2 * r) ** 2
         t_dadd = dp_adds * pts / rate
         grid2 = {"value": round(world * fl_g / per_g / 1e9, 3), "unit": "GFLOP/s", "steps": g_steps,

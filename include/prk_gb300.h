@@ -265,12 +265,13 @@ int prk_gb300_selftest_timeout(void);
 int prk_gb300_probe_dadd(double* adds_per_second);
 
 /* How the FP64 form of a stencil whose weights are not powers of two (star R=3..5, grid R=2..5) splits
- * the rounded adds of one application per interior point on whole-number tiles: *fixed_adds run in
- * exact fixed point on the integer pipes, *binary64_adds on the binary64 pipe (the rest of the
- * reference's chain and the add into out). Both give the reference's bits; the split sets the
- * kernel's two arithmetic ceilings. PRK_ERR_ARG for the power-of-two stencils. No counterpart in the
- * reference. */
-int prk_gb300_route_split(int pattern, int radius, int* fixed_adds, int* binary64_adds);
+ * the rounded adds of one application per interior point on whole-number tiles, in launches of
+ * `depth` applications (1: one application per launch; more: temporal blocking or a whole run, which
+ * move a larger share to the integer pipes): *fixed_adds run in exact fixed point on the integer
+ * pipes, *binary64_adds on the binary64 pipe (the rest of the reference's chain and the add into
+ * out). Both give the reference's bits; the split sets the kernel's two arithmetic ceilings.
+ * PRK_ERR_ARG for the power-of-two stencils or a depth below 1. No counterpart in the reference. */
+int prk_gb300_route_split(int pattern, int radius, int depth, int* fixed_adds, int* binary64_adds);
 
 /* Frees the device buffers and streams prk_gb300_run_host keeps on the current device. */
 int prk_gb300_release(void);

@@ -101,11 +101,12 @@ def probe_dadd() -> float:
     return res.value
 
 
-def route_split(pattern: int, radius: int) -> tuple[int, int] | None:
-    """(fixed-point adds, binary64 adds) per interior point and application of the FP64 table route
-    (prk_gb300_route_split), or None for the power-of-two stencils, which take the exact routes."""
+def route_split(pattern: int, radius: int, depth: int = 1) -> tuple[int, int] | None:
+    """(fixed-point adds, binary64 adds) per interior point and application of the FP64 table route in
+    launches of `depth` applications (prk_gb300_route_split), or None for the power-of-two stencils,
+    which take the exact routes."""
     f, d = C.c_int(), C.c_int()
-    rc = load().prk_gb300_route_split(pattern, radius, C.byref(f), C.byref(d))
+    rc = load().prk_gb300_route_split(pattern, radius, depth, C.byref(f), C.byref(d))
     return None if rc != 0 else (f.value, d.value)
 
 

@@ -44,7 +44,7 @@ SIGNATURES: dict[str, tuple] = {
     "prk_gb300_batch_launches": (_int, [_vp, _int]),
     "prk_gb300_batch_destroy": (_int, [_vp]),
     "prk_gb300_probe_dadd": (_int, [_pd]),
-    "prk_gb300_route_split": (_int, [_int, _int, _pi, _pi]),
+    "prk_gb300_route_split": (_int, [_int, _int, _int, _pi, _pi]),
     "prk_gb300_release": (_int, []),
     "prk_gb300_nstream": (_int, [_i64, _dbl, _vp, _vp, _vp, _vp]),
     "prk_gb300_transpose": (_int, [_i64, _vp, _vp, _vp]),

@@ -55,12 +55,13 @@ def launches_per_run(iterations: int, depth: int) -> int:
     return iterations // depth + bin(iterations % depth).count("1")
 
 
-def binary64_adds_per_point(pattern: int, r: int) -> int:
-    """Rounded binary64 adds one FP64 application issues per interior point on whole-number tiles: for
-    the stencils whose weights are not powers of two, the part of the reference's chain the table
-    route leaves on the binary64 pipe plus the add into out (prk_gb300_route_split); the power-of-two
-    stencils need none on the certified routes, where the sum is exact."""
-    split = kg.route_split(pattern, r)
+def binary64_adds_per_point(pattern: int, r: int, depth: int = 1) -> int:
+    """Rounded binary64 adds one FP64 application issues per interior point on whole-number tiles, in
+    launches of `depth` applications: for the stencils whose weights are not powers of two, the part
+    of the reference's chain the table route leaves on the binary64 pipe plus the add into out
+    (prk_gb300_route_split); the power-of-two stencils need none on the certified routes, where the
+    sum is exact."""
+    split = kg.route_split(pattern, r, depth)
     return 0 if split is None else split[1]
 
 
@@ -109,12 +110,13 @@ def one_case(torch, pattern: int, r: int, n: int, iterations: int, dtype: int, p
            "norm": nrm, "norm_ok": abs(nrm - 2.0 * (iterations + 1)) <= 1e-8,
            "tuning": {k: tuning[k] for k in ("depth", "kernel", "tile_rows", "tile_cols", "cols_per_thread")},
            "wall_s": round(wall, 3)}
-    adds = binary64_adds_per_point(pattern, r) if dtype == kg.FP64 else 0
+    launch_depth = 1 if d == 1 else max(2, iterations // nl)  # d = 0: the whole run in one launch
+    adds = binary64_adds_per_point(pattern, r, launch_depth) if dtype == kg.FP64 else 0
     if adds:
         rate = dadd_rate()
         t_adds = adds * (n - 2 * r) ** 2 / rate
         rec["roofline"]["binary64_add_ceiling"] = {
-            "adds_per_point": adds, "fixed_point_adds_per_point": kg.route_split(pattern, r)[0],
+            "adds_per_point": adds, "fixed_point_adds_per_point": kg.route_split(pattern, r, launch_depth)[0],
             "measured_adds_per_s": round(rate, 1),
             "ms_per_application": round(t_adds * 1e3, 4), "frac": round(t_adds / per_app, 4)}
     del in_a, in_b, out, res

@@ -245,12 +245,13 @@ int prk_gb300_probe_dadd(double* adds_per_second)
     return rc;
 }
 
-int prk_gb300_route_split(int pattern, int radius, int* fixed_adds, int* binary64_adds)
+int prk_gb300_route_split(int pattern, int radius, int depth, int* fixed_adds, int* binary64_adds)
 {
     if (!fixed_adds || !binary64_adds) return fail(PRK_ERR_ARG, "null output");
     if (pattern != PRK_STAR && pattern != PRK_GRID) return fail(PRK_ERR_ARG, "pattern %d is not PRK_STAR or PRK_GRID", pattern);
     if (radius < 1 || radius > prk::RMAX) return fail(PRK_ERR_ARG, "radius %d outside 1..5", radius);
-    if (prk::table_route_split(pattern, radius, fixed_adds, binary64_adds) != 0)
+    if (depth < 1) return fail(PRK_ERR_ARG, "depth %d is not positive", depth);
+    if (prk::table_route_split(pattern, radius, depth, fixed_adds, binary64_adds) != 0)
         return fail(PRK_ERR_ARG, "the weights of this stencil are powers of two: its FP64 form takes the exact routes");
     return PRK_OK;
 }

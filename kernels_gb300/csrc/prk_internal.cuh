@@ -78,9 +78,10 @@ cudaError_t launch_dadd_probe(double* sink, int blocks, int iters, double step, 
 unsigned long long current_context_id();
 
 // The table route's split of one application's adds per point for an FP64 stencil whose weights are
-// not powers of two: adds done in fixed point on the integer pipes and rounded binary64 adds (the rest
-// of the chain and the add into out). -1 for the other stencils (tile_host.cu).
-int table_route_split(int pattern, int R, int* fixed_adds, int* binary64_adds);
+// not powers of two, in launches of `depth` applications (1, or more): adds done in fixed point on the
+// integer pipes and rounded binary64 adds (the rest of the chain and the add into out). -1 for the
+// other stencils (tile_host.cu).
+int table_route_split(int pattern, int R, int depth, int* fixed_adds, int* binary64_adds);
 
 // Records `msg` as the calling thread's prk_gb300_last_error() and returns `code` (capi.cu).
 int record_error(int code, const char* msg);

@@ -772,29 +772,38 @@ static_assert(strict_taps_ok<STAR, 3>() && strict_taps_ok<STAR, 4>() && strict_t
                   strict_taps_ok<GRID, 5>(),
               "strict tap groups");
 
-// Sixteenths of each chain that run in fixed point (the rest stays on the binary64 pipe), per
-// pattern, as measured best at n=16384 (star 11, grid 9; 7 to 13 were within a few percent).
-#ifndef PRK_FX_SIXTEENTHS_STAR
-#define PRK_FX_SIXTEENTHS_STAR 11
-#endif
-#ifndef PRK_FX_SIXTEENTHS_GRID
-#define PRK_FX_SIXTEENTHS_GRID 9
-#endif
-
-template <int P, int R>
-constexpr int fixed_taps()
+// Sixteenths of each chain that run in fixed point (the rest stays on the binary64 pipe), per stencil
+// and form (ONE: one application per launch; else several, where the tile's load is shared by the
+// applications and the integer pipes take more of the chain), as measured best at n=16384 among 7
+// to 13 sixteenths (GFLOP/s, best against the next best):
+//  - one application: stars 9/16 (R=4: 1899 against 1852 at 10/16), 10/16 for R=3 (1804 against
+//    1784); grids 9/16 for R=2, 3 (2356 against 2317 at 11/16), 11/16 for R=4, 5 (2033 against 1986
+//    for R=5);
+//  - several: 11/16 (whole runs of 20: star R=3 2247 against 2204 at 12/16, grid R=2 2946 against
+//    2791 at 12/16 and 2610 at 9/16).
+template <int P, int R, bool ONE>
+__host__ __device__ constexpr int fixed_sixteenths()
 {
-    const int k = tap_count(P, R) * (P == STAR ? PRK_FX_SIXTEENTHS_STAR : PRK_FX_SIXTEENTHS_GRID) / 16;
+    if (!ONE) return 11;
+    if (P == STAR) return R == 3 ? 10 : 9;
+    return R <= 3 ? 9 : 11;
+}
+
+// Taps of each chain whose adds run in fixed point (at least the first).
+template <int P, int R, bool ONE>
+__host__ __device__ constexpr int fixed_taps()
+{
+    const int k = tap_count(P, R) * fixed_sixteenths<P, R, ONE>() / 16;
     return k < 1 ? 1 : (k > tap_count(P, R) ? tap_count(P, R) : k);
 }
 
 // True when a positive weight lies among the fixed taps: then the fixed part never sums to -0 (a
 // rounded sum is -0 only when every term is -0, and w * v with w > 0 is never -0).
-template <int P, int R>
+template <int P, int R, bool ONE>
 constexpr bool fixed_prefix_has_positive()
 {
     constexpr StrictTaps<P, R> t = make_strict_taps<P, R>();
-    for (int k = 0; k < fixed_taps<P, R>(); ++k)
+    for (int k = 0; k < fixed_taps<P, R, ONE>(); ++k)
         if (!t.neg[k]) return true;
     return false;
 }
@@ -856,15 +865,15 @@ __device__ __forceinline__ bool table_row_active(bool has_out, int64_t gi, int64
 }
 
 // The chain S of the points (r, c) and (r, c + 32): the reference's sum of fl(w * v) over the taps in
-// the generator's order, its first fixed_taps() adds in fixed point. sp points at the int32 tile's
-// (r, c) (row stride SW); the tables cover [base, base + TBL_L).
-template <int P, int R, int SW>
+// the generator's order, the adds of its first fixed_taps<P, R, ONE>() taps in fixed point. sp points
+// at the int32 tile's (r, c) (row stride SW); the tables cover [base, base + TBL_L).
+template <int P, int R, int SW, bool ONE>
 __device__ __forceinline__ void table_chain(const int32_t* sp, const uint64_t* T64, const uint4* T96, int base,
                                             double (&d)[2])
 {
     constexpr StrictTaps<P, R> TP = make_strict_taps<P, R>();
-    constexpr int N = tap_count(P, R), KF = fixed_taps<P, R>();
-    constexpr bool POS = fixed_prefix_has_positive<P, R>();
+    constexpr int N = tap_count(P, R), KF = fixed_taps<P, R, ONE>();
+    constexpr bool POS = fixed_prefix_has_positive<P, R, ONE>();
     uint32_t x[2][3];
     int anyv[2] = {0, 0};
 #pragma unroll
@@ -935,8 +944,8 @@ __device__ __forceinline__ void advance_i32_to(const int32_t* src, int32_t* dst)
 // the other sources o_s is scratch, filled from the out array (out_g points at the tile's (0, 0),
 // row stride n) before the first application and written back after the last, each thread its own
 // points. Returns false, having done nothing, when the values span TBL_L or more (lo and hi are
-// block-uniform).
-template <int P, int R, int SW, int SH, int TW, int ROWS, int OUT_SRC>
+// block-uniform). ONE: the launch applies the stencil once (the fixed-point share of one application).
+template <int P, int R, int SW, int SH, int TW, int ROWS, int OUT_SRC, bool ONE>
 __device__ __forceinline__ bool table_tile(int32_t* si, uint64_t* o_s, uint64_t* out_g, unsigned char* tbl, int lo,
                                            int hi, int nsteps, int64_t i0, int64_t j0, int64_t n, int64_t goff,
                                            int64_t row_end, bool has_out, int* fin)
@@ -979,7 +988,7 @@ __device__ __forceinline__ bool table_tile(int32_t* si, uint64_t* o_s, uint64_t*
             const int64_t gi = i0 + r;
             if (!table_row_active(has_out, gi, gi + goff, row_end, n, R)) continue;  // warp-uniform
             double d[2];
-            table_chain<P, R, SW>(s0 + r * SW + lane, T64, T96, base, d);
+            table_chain<P, R, SW, ONE>(s0 + r * SW + lane, T64, T96, base, d);
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 const int c = lane + 32 * h;
@@ -1214,7 +1223,7 @@ __device__ __forceinline__ void process_tile(unsigned char* stage, int* s_red, i
             }
             // kernels that keep out in HBM give the route an out area right after the tables
             uint64_t* o_s = OUT_SRC == OUT_SMEM ? o_tile : reinterpret_cast<uint64_t*>(tbl + table_bytes<P, R, DT>());
-            tbl_done = table_tile<P, R, G::SW, G::SH, C::TW, ROWS, OUT_SRC>(
+            tbl_done = table_tile<P, R, G::SW, G::SH, C::TW, ROWS, OUT_SRC, STEPS == 1>(
                 reinterpret_cast<int32_t*>(s_in), o_s, static_cast<uint64_t*>(out_v) + i0 * n + j0, tbl, lo, hi,
                 nsteps, i0, j0, n, goff, row_end, has_out, &iw_fin);
         }
@@ -1576,8 +1585,13 @@ template <int P, int R, int DT, int STEPS, int TH_>
 constexpr int min_blocks()
 {
     // the table route: three tiles per SM (80 registers), so that 24 warps hide the fixed-point
-    // chains' latencies (at four, 64 registers, the longer chains spill)
-    if (DT == FP64 && !pow2_weights(P, R)) return STEPS == 1 ? PRK_STRICT_BLOCKS_1 : PRK_STRICT_BLOCKS_N;
+    // chains' latencies (at four, 64 registers, the longer chains spill); tiles whose shared memory
+    // (tile and tables) admits at most two per SM get the registers of two (the 64-row tiles of grid
+    // R=3..5: at three, grid R=5 spilled 3 KB)
+    if (DT == FP64 && !pow2_weights(P, R)) {
+        if (SMEM_PER_SM / (tile_smem<P, R, DT, TH_>() + 1024) < 3) return 2;
+        return STEPS == 1 ? PRK_STRICT_BLOCKS_1 : PRK_STRICT_BLOCKS_N;
+    }
     if (DT == FP32C && P == GRID && R >= 3) return 2;  // bound by FP32 issue: registers over residency
     const int b = Geo<DT, R, TH_>::CTAS;
     if (STEPS == 1) return b;

@@ -82,15 +82,15 @@ bool tma_eligible(const StencilCall& c)
 
 bool tma_depth_ok(int steps) { return steps == 1 || steps == 2 || steps == 4 || steps == 8; }
 
-int table_route_split(int pattern, int R, int* fixed_adds, int* binary64_adds)
+int table_route_split(int pattern, int R, int depth, int* fixed_adds, int* binary64_adds)
 {
     int kf = -1, n = 0;
-#define PRK_SPLIT(PP, RR)                                              \
-    if (pattern == PP && R == RR) {                                    \
-        if constexpr (tile::table_route<PP, RR, FP64>()) {              \
-            kf = tile::fixed_taps<PP, RR>();                            \
-            n = tap_count(PP, RR);                                      \
-        }                                                               \
+#define PRK_SPLIT(PP, RR)                                                                            \
+    if (pattern == PP && R == RR) {                                                                  \
+        if constexpr (tile::table_route<PP, RR, FP64>()) {                                            \
+            kf = depth == 1 ? tile::fixed_taps<PP, RR, true>() : tile::fixed_taps<PP, RR, false>();    \
+            n = tap_count(PP, RR);                                                                    \
+        }                                                                                             \
     }
     PRK_SPLIT(STAR, 1) PRK_SPLIT(STAR, 2) PRK_SPLIT(STAR, 3) PRK_SPLIT(STAR, 4) PRK_SPLIT(STAR, 5)
     PRK_SPLIT(GRID, 1) PRK_SPLIT(GRID, 2) PRK_SPLIT(GRID, 3) PRK_SPLIT(GRID, 4) PRK_SPLIT(GRID, 5)
