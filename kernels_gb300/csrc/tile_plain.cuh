@@ -97,9 +97,10 @@ __device__ __forceinline__ void stage_async(unsigned char* smem, const void* in_
     __syncthreads();
 }
 
-// blockIdx = (tile column, tile row counted from row0). The evaluation is compiled for one-by-one
-// stores only (the shapes here never allow the 16-byte vectors). The arrays hold nr rows of the
-// n x n grid from grid row goff; rows from row_end on are read as halo but not stored.
+// blockIdx = (tile column, tile row counted from row0). The evaluation stores 16-byte vectors only
+// on the rows whose words start on a 16-byte boundary (vec_ok false: checked row by row), the other
+// rows one element at a time. The arrays hold nr rows of the n x n grid from grid row goff; rows
+// from row_end on are read as halo but not stored.
 // The stencils that take the table route stage `in` and `out` with asynchronous copies and update
 // `out` in the shared-memory out tile (n=16383, FP64, one application: star R=3 1620 GFLOP/s against
 // 1472 with `in` staged by plain loads and `out` read by the table route itself, grid R=2 2246
