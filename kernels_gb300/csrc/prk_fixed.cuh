@@ -166,35 +166,13 @@ PRK_HD uint64_t mul_whole20(uint64_t wb, int32_t v)
 // reference's chain (((p1 + p2) + p3) + ...). On tiles of whole numbers |v| < 2^20 every product
 // p = fl(w * v) of a PRK weight (|w| >= 1/900) is a multiple of 2^-62 (its lowest bit lies at most 52
 // places below its leading bit, which is at or above 2^-10), and every partial sum, being the rounded
-// sum of such multiples, is one too; all stay below 2^22 in magnitude (sum |w| <= 2). Each value is
-// then an integer of units 2^-62 below 2^84, held exactly in three 32-bit words as a two's-complement
-// number, and a rounded binary64 add is: the exact integer sum, then rounding to 53 significant bits
-// at the position its leading bit sets, to nearest with ties to the even neighbour. Both steps are
-// integer instructions, so a chain can leave the binary64 pipe for the integer pipes and come back
-// with the same bits (fx96_to_bits).
+// sum of such multiples, is one too; all stay below 2^21 in magnitude (sum |w| <= 1.5, for grid
+// R=2). Each value is then an integer of units 2^-62 below 2^83, held exactly in three 32-bit words
+// as a two's-complement number, and a rounded binary64 add is: the exact integer sum, then rounding
+// to 53 significant bits at the position its leading bit sets, to nearest with ties to the even
+// neighbour. Both steps are integer instructions, so a chain can leave the binary64 pipe for the
+// integer pipes and come back with the same bits (fx96_to_bits).
 constexpr int FX96_F = 62;
-
-PRK_HD float f32_from_bits(uint32_t u)
-{
-#ifdef __CUDA_ARCH__
-    return __uint_as_float(u);
-#else
-    float f;
-    std::memcpy(&f, &u, 4);
-    return f;
-#endif
-}
-
-PRK_HD uint32_t f32_bits(float f)
-{
-#ifdef __CUDA_ARCH__
-    return __float_as_uint(f);
-#else
-    uint32_t u;
-    std::memcpy(&u, &f, 4);
-    return u;
-#endif
-}
 
 // x = v * 2^62 for a binary64 v (encoding b) with |v| < 2^22 that is a multiple of 2^-62, or +-0.
 PRK_HD void fx96_from_bits(uint64_t b, uint32_t& x0, uint32_t& x1, uint32_t& x2)
@@ -222,10 +200,10 @@ PRK_HD void fx96_from_bits(uint64_t b, uint32_t& x0, uint32_t& x1, uint32_t& x2)
     x2 = hi;
 }
 
-// x = fl(x + p) (SUB: fl(x - p)) for 96-bit fixed-point values whose exact result lies below 2^84
-// units: the exact sum, then rounding to 53 significant bits, nearest-even. The position b of the
-// rounding is the leading bit of |sum| less 52, at most 31, so only the low word is cut and the
-// rounding increment carries into the others. Rounding the two's-complement value to a multiple of
+// x = fl(x + p) (SUB: fl(x - p)) for 96-bit fixed-point values whose exact result lies below 2^83
+// units (values below 2^21): the exact sum, then rounding to 53 significant bits, nearest-even. The
+// position b of the rounding is the leading bit of |sum| less 52, at most 30, so only the low word
+// is cut and the rounding increment carries into the others. Rounding the two's-complement value to a multiple of
 // 2^b with ties to the even multiple gives the same result as rounding its magnitude and negating;
 // the leading bit is read from the one's complement of a negative sum, which differs from the
 // magnitude's only when the magnitude is a power of two (then nothing lies below b anyway).
@@ -249,17 +227,20 @@ PRK_HD void fx96_acc_round(uint32_t& x0, uint32_t& x1, uint32_t& x2, uint32_t p0
     x0 = static_cast<uint32_t>(r);
     x1 = static_cast<uint32_t>(r >> 32);
 #endif
-    // b = max(0, msb|sum| - 52). The leading bit is read from the one's complement of a negative sum
-    // (t2:t1 below), and its position from the exponent of an exact float: float(t2) when the high
-    // word is not zero (t2 < 2^20: b = msb(t2) + 12), else float(t1 >> 9) (b = msb(t1 >> 9) - 11, and 0
-    // for anything smaller), each converted with the 2^23 magic number (no leading-zero count, which
-    // issues at a quarter of the integer rate).
-    const uint32_t sg = static_cast<uint32_t>(static_cast<int32_t>(x2) >> 31);
-    const uint32_t t2 = x2 ^ sg, t1 = x1 ^ sg;
-    const uint32_t y = t2 ? t2 : (t1 >> 9);
-    const int off = t2 ? 115 : 138;
-    const int b0 = static_cast<int>(f32_bits(f32_from_bits(0x4B000000u | y) - 8388608.0f) >> 23) - off;
-    const int b = b0 < 0 ? 0 : b0;
+    // b = max(0, msb|sum| - 52). As |sum| < 2^83, bits 83 and up are copies of the sign, so bits
+    // 52..83 of the sum are one signed 32-bit word z = sum >> 52 (a funnel shift of the top two
+    // words), and the position of z's most significant bit that differs from its sign bit (bfind.s32;
+    // -1 when there is none, for z = 0 or -1) is msb|sum| - 52, read for a negative sum from its one's
+    // complement.
+    const uint32_t z = (x2 << 12) | (x1 >> 20);
+#ifdef __CUDA_ARCH__
+    int f;
+    asm("bfind.s32 %0, %1;" : "=r"(f) : "r"(z));
+#else
+    const uint32_t zm = static_cast<int32_t>(z) < 0 ? ~z : z;
+    const int f = zm ? 31 - clz32(zm) : -1;
+#endif
+    const int b = f < 0 ? 0 : f;
     // round to a multiple of 2^b, nearest-even: add 2^(b-1) - 1 and the lowest kept bit, then cut
     const uint32_t mask = (1u << b) - 1u;
     const uint32_t hq = (mask >> 1) + ((x0 >> b) & (mask & 1u));
