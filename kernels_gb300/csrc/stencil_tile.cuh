@@ -774,19 +774,20 @@ static_assert(strict_taps_ok<STAR, 3>() && strict_taps_ok<STAR, 4>() && strict_t
 
 // Sixteenths of each chain that run in fixed point (the rest stays on the binary64 pipe), per stencil
 // and form (ONE: one application per launch; else several, where the tile's load is shared by the
-// applications and the integer pipes take more of the chain), as measured best at n=16384 among 7
-// to 13 sixteenths (GFLOP/s, best against the next best):
-//  - one application: stars 9/16 (R=4: 1899 against 1852 at 10/16), 10/16 for R=3 (1804 against
-//    1784); grids 9/16 for R=2, 3 (2356 against 2317 at 11/16), 11/16 for R=4, 5 (2033 against 1986
-//    for R=5);
-//  - several: 11/16 (whole runs of 20: star R=3 2247 against 2204 at 12/16, grid R=2 2946 against
-//    2791 at 12/16 and 2610 at 9/16).
+// applications and the integer pipes take more of the chain), as measured best at n=16384 among 9 to
+// 15 sixteenths (GFLOP/s, best against the next best):
+//  - one application: star R=3 10/16 (1994 against 1972 at 12/16), R=4, 5 12/16 (2066 against 2031
+//    at 13/16 for R=5); grid R=2, 3 12/16 (2869 against 2826 at 13/16 for R=3), R=4 13/16 (2727
+//    against 2706), R=5 15/16 (2657 against 2621);
+//  - several (whole runs of 20): star R=3 12/16 (2714 against 2510 at 11/16), R=4, 5 13/16 (2929
+//    against 2887 for R=5); grid R=2, 3 12/16 (3616 against 3557 at 13/16 for R=2), R=4, 5 13/16
+//    (3222 against 3148 for R=5).
 template <int P, int R, bool ONE>
 __host__ __device__ constexpr int fixed_sixteenths()
 {
-    if (!ONE) return 11;
-    if (P == STAR) return R == 3 ? 10 : 9;
-    return R <= 3 ? 9 : 11;
+    if (P == STAR) return ONE ? (R == 3 ? 10 : 12) : (R == 3 ? 12 : 13);
+    if (R <= 3) return 12;
+    return ONE && R == 5 ? 15 : 13;
 }
 
 // Taps of each chain whose adds run in fixed point (at least the first).

@@ -36,16 +36,15 @@ def test_version_and_pure_functions():
 def test_route_split_covers_every_add_of_the_chain():
     """prk_gb300_route_split: for the stencils whose weights are not powers of two, the fixed-point
     and binary64 adds of one application per point are the chain's taps - 1 adds plus the add into
-    out, in launches of one application and of several; most of each chain runs in fixed point, and
-    no less of it in multi-application launches. The power-of-two stencils, a radius outside 1..5 and
-    a depth below 1 are rejected."""
+    out, in launches of one application and of several (one split for every depth above 1); most of
+    each chain runs in fixed point. The power-of-two stencils, a radius outside 1..5 and a depth below
+    1 are rejected."""
     for p, r in [(kg.STAR, 3), (kg.STAR, 4), (kg.STAR, 5), (kg.GRID, 2), (kg.GRID, 3), (kg.GRID, 4), (kg.GRID, 5)]:
         taps = 4 * r if p == kg.STAR else 4 * r * r + 2 * r
         one, many = kg.route_split(p, r, 1), kg.route_split(p, r, 8)
         for fixed, dp in (one, many):
             assert fixed + dp == taps, (p, r)
             assert taps // 2 <= fixed < taps and dp >= 2
-        assert many[0] >= one[0], (p, r)
         assert kg.route_split(p, r, 100) == many
     for p, r in [(kg.STAR, 1), (kg.STAR, 2), (kg.GRID, 1)]:
         assert kg.route_split(p, r) is None
