@@ -776,18 +776,21 @@ static_assert(strict_taps_ok<STAR, 3>() && strict_taps_ok<STAR, 4>() && strict_t
 // and form (ONE: one application per launch; else several, where the tile's load is shared by the
 // applications and the integer pipes take more of the chain), as measured best at n=16384 among 9 to
 // 15 sixteenths (GFLOP/s, best against the next best):
-//  - one application: star R=3 10/16 (1994 against 1972 at 12/16), R=4, 5 12/16 (2066 against 2031
-//    at 13/16 for R=5); grid R=2, 3 12/16 (2869 against 2826 at 13/16 for R=3), R=4 13/16 (2727
-//    against 2706), R=5 15/16 (2657 against 2621);
-//  - several (whole runs of 20): star R=3 12/16 (2714 against 2510 at 11/16), R=4, 5 13/16 (2929
-//    against 2887 for R=5); grid R=2, 3 12/16 (3616 against 3557 at 13/16 for R=2), R=4, 5 13/16
-//    (3222 against 3148 for R=5).
+//  - one application: star R=3, 4 11/16 (2150 against 2098 at 12/16 for R=4), R=5 12/16 (2066
+//    against 2031 at 13/16); grid R=2 11/16 (2745 against 2704 at 12/16), R=3 12/16 (2870 against
+//    2859 at 11/16), R=4 13/16 (2728 against 2721 at 14/16), R=5 15/16 (2656 against 2621 at 13/16);
+//  - several (whole runs of 20): star R=3 14/16 (2777 against 2714 at 12/16), R=4, 5 13/16 (2930
+//    against 2898 at 14/16 for R=5); grid R=2, 3 12/16 (3616 against 3557 at 13/16 for R=2), R=4
+//    14/16 (3444 against 3419 at 13/16), R=5 13/16 (3222 against 3148 at 12/16).
 template <int P, int R, bool ONE>
 __host__ __device__ constexpr int fixed_sixteenths()
 {
-    if (P == STAR) return ONE ? (R == 3 ? 10 : 12) : (R == 3 ? 12 : 13);
-    if (R <= 3) return 12;
-    return ONE && R == 5 ? 15 : 13;
+    if (P == STAR) {
+        if (ONE) return R == 5 ? 12 : 11;
+        return R == 3 ? 14 : 13;
+    }
+    if (ONE) return R == 2 ? 11 : (R == 3 ? 12 : (R == 4 ? 13 : 15));
+    return R <= 3 ? 12 : (R == 4 ? 14 : 13);
 }
 
 // Taps of each chain whose adds run in fixed point (at least the first).
